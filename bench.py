@@ -1,0 +1,328 @@
+"""Benchmark: weighted model counts/sec on a sliced cubic vertex-cover plan.
+
+Workload: weighted cubic vertex cover, seeded random 3-regular graph, n=220
+vertices / 330 edge clauses, cachet weights p ~ U(0.3, 0.7), line-Flow plan
+sliced into 2^10 equal-shape slices (frozen in
+``tensororder_gb300/plans/wvc220_s10.json.gz`` with the reference's own count).
+One step = one complete weighted count (all 1024 slices, compensated FP64 slice
+sum).  ``value`` is counts/sec of the chosen (split) form with the plan already
+resident on the device; ``e2e`` is the same metric through the plugin's public
+call with host inputs (program upload, contraction, result read-back).
+
+``--impl reference`` times the reference algorithm on the host cores instead
+(the numpy FP64 restatement in ``oracle/``: the reference's compiled parts are
+not available on this machine), on a bounded sample of slices per step.
+"""
+import argparse
+import gzip
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "wvc220_s10"
+METRIC = "weighted counts/sec (chosen split form, all 1024 slices per count)"
+UNIT = "counts/s"
+
+
+def load_workload(name=WORKLOAD):
+    from tensororder_gb300.program import Program
+
+    with gzip.open(os.path.join(ROOT, "tensororder_gb300", "plans", name + ".json.gz"), "rt") as f:
+        doc = json.load(f)
+    return doc, Program.from_dict(doc["program"])
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) != len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def cpu_baseline(prog, max_seconds=12.0, min_slices=2):
+    """The numpy restatement of the reference's contraction on this host's
+    cores, on a prefix sample of the slices (bounded by ``max_seconds``)."""
+    from oracle import contract as oracle
+
+    t0 = time.perf_counter()
+    n = 0
+    total = 0.0
+    while n < prog.num_slices and (n < min_slices or time.perf_counter() - t0 < max_seconds):
+        arr, _ = oracle.contract(prog, n)
+        total += float(arr[()])
+        n += 1
+    dt = time.perf_counter() - t0
+    per_slice = dt / n
+    return {"value": 1.0 / (per_slice * prog.num_slices), "unit": UNIT, "cores": os.cpu_count(),
+            "kind": "port",
+            "sample": "first %d of %d slices (%.1f s), numpy FP64 np.tensordot on all host BLAS threads, "
+                      "extrapolated to the full count" % (n, prog.num_slices, dt)}
+
+
+def run_reference(args, rank, world):
+    doc, prog = load_workload()
+    if rank != 0:
+        return
+    from oracle import contract as oracle
+
+    sample = max(1, args.ref_sample)
+    for _ in range(args.warmup):
+        oracle.contract(prog, 0)
+    times = []
+    for step in range(args.steps):
+        t0 = time.perf_counter()
+        for s in range(sample):
+            oracle.contract(prog, (step * sample + s) % prog.num_slices)
+        times.append((time.perf_counter() - t0) / sample)
+    per_slice = float(np.mean(times))
+    value = 1.0 / (per_slice * prog.num_slices)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_slice * prog.num_slices * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "slices": prog.num_slices, "joins": prog.num_joins,
+                   "per_step_sample_slices": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                         "sample": "%d slices per step of %d, numpy FP64 (the reference's np.tensordot "
+                                   "contraction restated over the same frozen plan), all host BLAS threads"
+                                   % (sample, prog.num_slices)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--ref-sample", type=int, default=8)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import torch.distributed as dist
+
+    from tensororder_gb300 import api, runtime
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    doc, prog = load_workload()
+    ref = doc["reference"]["float64"]
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+
+    dp = runtime.DeviceProgram(prog, local)
+    info = dp.info
+    S = prog.num_slices
+    flops = info.flops_per_slice * S
+    ws_split = dp.allocate_workspace(runtime.MODE_SPLIT, S, max_fraction=0.6)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    def one(mode, ws):
+        dp.reset(stream)
+        dp.run(mode, 0, S, workspace=ws, stream=stream)
+
+    def timed(mode, ws, steps, warmup):
+        for _ in range(warmup):
+            one(mode, ws)
+        torch.cuda.synchronize(dev)
+        ms = []
+        for _ in range(steps):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            one(mode, ws)
+            b.record(stream)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        val = float(dp.result(stream).reshape(-1)[0])  # the last step's count
+        return ms, val
+
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clocks:
+        split_ms, split_val = timed(runtime.MODE_SPLIT, ws_split, args.steps, args.warmup)
+    torch.cuda.synchronize(dev)
+    t_split = float(np.sum(split_ms)) / 1e3
+    if world > 1:
+        t = torch.tensor([t_split], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_split = float(t.item())
+    ms_split = t_split * 1e3 / args.steps
+
+    # Plain FP64 form on the same plan (the 10x comparison).
+    ws_plain = dp.allocate_workspace(runtime.MODE_F64, S, max_fraction=0.6)
+    plain_ms, plain_val = timed(runtime.MODE_F64, ws_plain, args.plain_steps, 1)
+    ms_plain = float(np.mean(plain_ms))
+
+    # Per-join device times of one instrumented pass of each form (CUDA events
+    # between launches on the launching stream).
+    def per_join(mode, ws):
+        dp.set_timing(True)
+        one(mode, ws)
+        torch.cuda.synchronize(dev)
+        t = dp.join_times()
+        dp.set_timing(False)
+        return t
+
+    from oracle import contract as oracle  # checker only: shapes of the joins
+
+    shapes = oracle.join_shapes(prog)
+    jt_split = per_join(runtime.MODE_SPLIT, dp.allocate_workspace(runtime.MODE_SPLIT, S, 0.6))
+    jt_plain = per_join(runtime.MODE_F64, dp.allocate_workspace(runtime.MODE_F64, S, 0.6))
+    top = int(np.argmax(jt_split))
+    m, n, k = shapes[top]
+    top_flops = 2.0 * m * n * k * S
+    top_bytes = 4.0 * (m * k + k * n + m * n) * S
+    fp32_peak = runtime.probe_peak(1, stream)
+    fp64_peak = runtime.probe_peak(0, stream)
+    peaks = measured_peaks()
+
+    # End to end through the plugin's public call: host program in, count out.
+    backend = api.GB300SplitAPI(device=local)
+    e2e_ms = []
+    for i in range(args.warmup + max(3, args.steps // 2)):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        val = float(backend.contract_program(prog))
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_ms.append((t1 - t0) * 1e3)
+    h2d = int(sum((1 << l.rank) * 12 for l in prog.leaves))  # FP64 + FP32 leaf copies
+    d2h = 16 * (1 << int(info.root_rank))
+
+    line = {
+        "metric": METRIC,
+        "value": world * 1e3 / ms_split,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_split,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+pow2-exponent (FP64 compensated slice sum)",
+        "data": "synthetic (seeded 3-regular graph, frozen reference plan)",
+        "config": {
+            "workload": "weighted cubic vertex cover n=220 (330 clauses), line-Flow, 2^10 slices",
+            "slices": S, "joins": prog.num_joins, "max_rank": int(info.max_rank),
+            "algorithmic_flop_per_count": flops,
+            "l2": "512 MiB buffer zeroed between timed steps (L2 is 129 MB)",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+        },
+        "tflops": flops / (ms_split * 1e-3) / 1e12,
+        "rel_err": abs(split_val - ref) / ref,
+        "plain_f64": {"ms_per_count": ms_plain, "counts_per_s": 1e3 / ms_plain,
+                      "tflops": flops / (ms_plain * 1e-3) / 1e12, "rel_err": abs(plain_val - ref) / ref},
+        "speedup_chosen_vs_plain": ms_plain / ms_split,
+        "roofline": {
+            "kernel": "join %d (M,N,K)=(%d,%d,%d) x %d slices, split form" % (top, m, n, k, S),
+            "bound": "fp32-fma",
+            "achieved": top_flops / (jt_split[top] * 1e-3) / 1e12,
+            "peak": fp32_peak / 1e12,
+            "unit": "TFLOP/s",
+            "frac": (top_flops / (jt_split[top] * 1e-3)) / fp32_peak,
+            "peak_source": "togb_probe_peak FP32 FMA chain, measured in this run",
+            "hbm_achieved_gbs": top_bytes / (jt_split[top] * 1e-3) / 1e9,
+            "hbm_peak_gbs": peaks.get("hbm_gbs"),
+            "share_of_step": float(jt_split[top] / jt_split.sum()),
+            "traffic": None,
+        },
+        "fp64_roofline": {"achieved_tflops": flops / (ms_plain * 1e-3) / 1e12, "peak_tflops": fp64_peak / 1e12,
+                          "frac": (flops / (ms_plain * 1e-3)) / fp64_peak,
+                          "peak_source": "togb_probe_peak FP64 FMA chain, measured in this run"},
+        "clocks": clocks.summary(),
+        "e2e": {"value": 1e3 / float(np.mean(e2e_ms)), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "path": "GB300SplitAPI.contract_program(host program) -> libtogb C ABI"},
+        "gpu_launches": int(info.num_launches) * args.steps,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(prog)
+    if world > 1:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,130 @@
+/*
+ * togb.h -- C ABI of the GB300 contraction backend for TensorOrder.
+ *
+ * The entry points replace the Execution stage of a TensorOrder plan:
+ *
+ *   togb_program_create / togb_program_run / togb_program_result
+ *       replace BaseTensorAPI.contract_sliced
+ *       (src/tensor_network/tensor_apis/base_api.py:17-28), which loops over
+ *       slices (TensorNetwork.slice_groups, src/tensor_network/tensor_network.pyx:363-401),
+ *       contracts each slice with TensorNetwork.identify
+ *       (src/tensor_network/tensor_network.pyx:142-156) and sums result[()]
+ *       in FP64.  The caller passes the plan flattened by the host side
+ *       (leaves, post-order tokens, slice groups); the library does the rest.
+ *   togb_tensordot_f64
+ *       replaces NumpyAPI.tensordot (src/tensor_network/tensor_apis/numpy_apis.py:42-43)
+ *       and TensorFlowAPI.tensordot (src/tensor_network/tensor_apis/tensorflow_apis.py:99-102)
+ *       for binary-index tensors already resident on the device.
+ *
+ * All pointers are plain host or device pointers; no framework types cross
+ * this boundary.  Every call returns a togb_status; togb_last_error() gives a
+ * message for the calling thread's most recent failure.  TOGB_ERR_OOM maps to
+ * the reference's OutOfMemoryError (base_api.py:4), whose handler re-slices
+ * the plan and retries (src/execution.py:134-142).
+ */
+#ifndef TOGB_H
+#define TOGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  TOGB_OK = 0,
+  TOGB_ERR_INVALID = 1,     /* malformed program or argument            */
+  TOGB_ERR_OOM = 2,         /* device allocation failed / workspace too small */
+  TOGB_ERR_CUDA = 3,        /* CUDA runtime error                         */
+  TOGB_ERR_UNSUPPORTED = 4, /* valid input outside what the kernels cover */
+  TOGB_ERR_TIMEOUT = 5      /* a device-side wait ran out of its budget   */
+} togb_status;
+
+typedef enum {
+  TOGB_MODE_F64 = 0,  /* plain form: FP64 storage and arithmetic          */
+  TOGB_MODE_SPLIT = 1 /* chosen form: FP32 storage with a per-slice power-of-two
+                         exponent per tensor; FP64 only in the slice sum  */
+} togb_mode;
+
+typedef struct togb_program togb_program;
+
+/* A flattened plan.  Leaf i has leaf_rank[i] axes whose edge ids follow in
+ * leaf_axes (the tensor's index_list order); its values are the 2^rank FP64
+ * entries of the unsliced tensor, row-major in that axis order, concatenated
+ * in leaf_values.  postorder holds a leaf index (push) or -1 (pop right, pop
+ * left, push their tensordot).  Slice group g lists group_size[g] edge ids in
+ * group_edges; slice s fixes the edges of group g to bit (num_groups-1-g) of s,
+ * which is itertools.product order over the groups. */
+typedef struct {
+  int32_t num_leaves;
+  const int32_t* leaf_rank;
+  const int32_t* leaf_axes;
+  const double* leaf_values;
+  int32_t num_tokens;
+  const int32_t* postorder;
+  int32_t num_groups;
+  const int32_t* group_size;
+  const int32_t* group_edges;
+} togb_program_desc;
+
+typedef struct {
+  int64_t num_slices;
+  int32_t num_joins;
+  int32_t max_rank;              /* largest tensor rank over unsliced axes     */
+  int32_t root_rank;             /* rank of the final tensor (0 for a count)   */
+  int32_t num_launches;          /* kernel launches per chunk of slices        */
+  double flops_per_slice;        /* sum over joins of 2*M*N*K                  */
+  double bytes_per_slice_f64;    /* sum over joins of 8*(M*K + K*N + M*N)      */
+  int64_t workspace_per_slice[2];/* workspace bytes per slice, by togb_mode    */
+  int64_t workspace_fixed[2];    /* workspace bytes independent of slice count */
+} togb_program_info;
+
+/* Lower and plan a program for `device`; copies the leaves to the device. */
+togb_status togb_program_create(const togb_program_desc* desc, int device, togb_program** out);
+
+togb_status togb_program_info_get(const togb_program* prog, togb_program_info* info);
+
+/* Zero the device-side slice accumulator (compensated FP64 sum). */
+togb_status togb_program_reset(togb_program* prog, void* stream);
+
+/* Contract slices [slice_begin, slice_end) in `mode` and add them into the
+ * accumulator.  `workspace` is device memory of `workspace_bytes`; when NULL
+ * the program allocates (and keeps) its own.  Slices are processed in chunks
+ * that fit the workspace.  Work is queued on `stream` (a cudaStream_t, NULL =
+ * legacy default stream); the call returns without waiting for it. */
+togb_status togb_program_run(togb_program* prog, int mode, int64_t slice_begin, int64_t slice_end,
+                             void* workspace, size_t workspace_bytes, void* stream);
+
+/* Wait for `stream` and copy the accumulated root tensor (2^root_rank
+ * entries, row-major in the reference's output axis order) to host `out`,
+ * together with the compensation terms (`comp`, may be NULL). */
+togb_status togb_program_result(togb_program* prog, void* stream, double* out, double* comp, int64_t n);
+
+/* Per-join device time of the last run with togb_program_set_timing(prog, 1):
+ * `ms[j]` for each join in post-order (n = num_joins). */
+togb_status togb_program_set_timing(togb_program* prog, int enable);
+togb_status togb_program_join_times(togb_program* prog, float* ms, int32_t n);
+
+void togb_program_destroy(togb_program* prog);
+
+/* out = np.tensordot(a, b, (axes_a, axes_b)) for binary-index FP64 tensors on
+ * the device (every dimension 2).  `out` must hold 2^(rank_a+rank_b-2*n_axes)
+ * doubles; its axes are a's free axes in order, then b's.  Asynchronous on
+ * `stream`. */
+togb_status togb_tensordot_f64(const double* a, int32_t rank_a, const double* b, int32_t rank_b,
+                               int32_t n_axes, const int32_t* axes_a, const int32_t* axes_b,
+                               double* out, void* stream);
+
+/* Device throughput probe used for roofline denominators: runs a dependent
+ * FMA chain kernel of `kind` (0 = FP64 FFMA, 1 = FP32 FFMA) and returns the
+ * achieved FLOP/s measured with CUDA events on `stream`. */
+togb_status togb_probe_peak(int kind, void* stream, double* flops_per_second);
+
+const char* togb_last_error(void);
+int togb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TOGB_H */

@@ -1,0 +1,166 @@
+"""The ``--tensor_library`` plugin: TensorOrder's Execution stage on a GB300.
+
+Mirrors the reference's backend interface (duck-typed, as ``tensororder.py``
+and ``execution.py`` use it): ``add_argument``, ``get_entry_size``,
+``create_tensor``, ``tensordot``, ``contract``, ``contract_sliced``, ``warm``
+(``tensor_apis/base_api.py:8-28``, ``tensor_apis/numpy_apis.py:4-65``,
+``tensor_apis/tensorflow_apis.py:51-133``).
+
+* ``gb300``       -- plain form: FP64 storage and arithmetic.
+* ``gb300-split`` -- chosen form: FP32 storage with per-slice power-of-two
+  exponents, FP64 only in the compensated slice sum.
+
+``contract_sliced`` is the hot path.  It flattens the plan
+(:func:`tensororder_gb300.program.from_plan`), hands it to libtogb and runs the
+slices in chunks: each C call returns after queueing a bounded number of
+slices, so the reference's SIGALRM timeouts (``util.py:13-122``) still fire
+between chunks.  A device allocation failure raises the reference's
+``OutOfMemoryError`` (``base_api.py:4``), whose handler in ``execution.py:134-142``
+re-slices the plan and retries.  Nothing here falls back to a CPU path: if the
+CUDA library or device is missing the call fails.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import program as _program
+from . import runtime
+
+
+class OutOfMemoryError(Exception):
+    """Stand-in for ``tensor_network.OutOfMemoryError`` until :func:`register`
+    binds the reference's class."""
+
+
+_OOM = OutOfMemoryError
+
+
+class GB300API:
+    """Execution backend; ``mode`` is ``runtime.MODE_F64`` or ``runtime.MODE_SPLIT``."""
+
+    slices_per_call = 1 << 14  # upper bound on slices queued by one C call
+
+    def __init__(self, mode=runtime.MODE_F64, device=0):
+        self._mode = mode
+        self._device = device
+        self._thread_limit = None
+        self.last_program = None
+
+    # -- configuration (numpy_apis.py:13-34) --------------------------------
+    def add_argument(self, key, value):
+        if key == "entry_type":
+            if value == "float64":
+                return
+            if value == "float32":
+                self._mode = runtime.MODE_SPLIT
+                return
+            raise ValueError("Unknown gb300 type %s" % value)
+        if key == "thread_limit":
+            # Host thread cap of the numpy backend; the device path has no host
+            # compute threads to limit.
+            self._thread_limit = value
+            return
+        raise ValueError("Invalid argument " + str(key) + " for selected tensor_library")
+
+    def get_entry_size(self):
+        return 8 if self._mode == runtime.MODE_F64 else 4
+
+    # -- tensor primitives ---------------------------------------------------
+    def create_tensor(self, shape, default_value=None):
+        """Host tensor for ``Tensor.build`` (leaves are built on the host and
+        uploaded once per program)."""
+        if default_value is None:
+            return np.empty(shape, dtype=np.float64)
+        return np.full(shape, default_value, dtype=np.float64)
+
+    def tensordot(self, a, b, axes):
+        """``np.tensordot`` on the device; numpy inputs are uploaded, the result
+        is a float64 CUDA tensor."""
+        import torch
+
+        dev = torch.device("cuda", self._device)
+
+        def as_dev(x):
+            if isinstance(x, torch.Tensor):
+                return x.to(device=dev, dtype=torch.float64)
+            return torch.as_tensor(np.asarray(x, dtype=np.float64), device=dev)
+
+        return runtime.tensordot_f64(as_dev(a), as_dev(b), axes)
+
+    def warm(self):
+        """Load the library and create the CUDA context with one tiny contraction."""
+        import torch
+
+        a = torch.full((2,), 2.0, dtype=torch.float64, device=torch.device("cuda", self._device))
+        runtime.tensordot_f64(a, a, ([0], [0]))
+        torch.cuda.synchronize(self._device)
+
+    # -- contraction ---------------------------------------------------------
+    def contract(self, network, contraction_tree):
+        """Contract one (already sliced or unsliced) network along a tree, as
+        ``NumpyAPI.contract`` (``numpy_apis.py:45-55``) does."""
+
+        class _Plan:
+            pass
+
+        plan = _Plan()
+        plan.network, plan.tree, plan.groups_to_slice = network, contraction_tree, []
+        return np.asarray(self._run(_program.from_plan(plan), None))
+
+    def contract_sliced(self, execution_plan, num_slice_limit=None):
+        """Sum of the contractions of every slice of the plan
+        (``base_api.py:17-28``); ``num_slice_limit`` keeps a prefix in
+        ``itertools.product`` order."""
+        value = self._run(_program.from_plan(execution_plan), num_slice_limit)
+        return value[()] if np.ndim(value) == 0 else value
+
+    def contract_program(self, prog, num_slice_limit=None):
+        """Same as ``contract_sliced`` for an already flattened program."""
+        value = self._run(prog, num_slice_limit)
+        return value[()] if np.ndim(value) == 0 else value
+
+    def _run(self, prog, num_slice_limit):
+        import torch
+
+        n = prog.num_slices if num_slice_limit is None else min(prog.num_slices, int(num_slice_limit))
+        try:
+            dp = runtime.DeviceProgram(prog, self._device)
+            self.last_program = dp
+            stream = torch.cuda.current_stream(self._device)
+            dp.reset(stream)
+            ws = dp.allocate_workspace(self._mode, max(n, 1))
+            s = 0
+            while s < n:
+                e = min(n, s + self.slices_per_call)
+                dp.run(self._mode, s, e, workspace=ws, stream=stream)
+                s = e
+            return dp.result(stream)
+        except runtime.DeviceOutOfMemory as exc:
+            raise _OOM(str(exc))
+
+
+class GB300SplitAPI(GB300API):
+    def __init__(self, device=0):
+        super().__init__(mode=runtime.MODE_SPLIT, device=device)
+
+
+GB300_APIS = {
+    "gb300": GB300API,
+    "gb300-split": GB300SplitAPI,
+}
+
+
+def register(all_apis=None):
+    """Add the plugins to the reference's ``tensor_network.ALL_APIS``.
+
+    ``--tensor_library`` is resolved through ``util.TaggedChoice`` over that
+    live dict (``util.py:249-252``), so registering before the CLI runs is all
+    the integration needed; no reference file is edited.
+    """
+    global _OOM
+    import tensor_network
+
+    _OOM = tensor_network.OutOfMemoryError
+    target = tensor_network.ALL_APIS if all_apis is None else all_apis
+    target.update(GB300_APIS)
+    return target

@@ -1,0 +1,73 @@
+// Internal descriptors shared by the host runtime and the CUDA kernels.
+//
+// A join of the flattened plan is one batched "deposit GEMM":
+//
+//     C[b][m, n] = sum_k A[b][m, k] * B[b][n, k]
+//
+// over the slices b of a chunk.  Every index is binary, so the element of an
+// operand at GEMM coordinates (outer, k) lives at
+//
+//     ptr + slice_offset(b) + sum_i bit_i(outer) * s_outer[i] + sum_i bit_i(k) * s_k[i]
+//
+// ("deposit" addressing).  That covers any axis permutation of either operand
+// without materialising a transpose (the TTGT transposes np.tensordot performs
+// in numpy_apis.py:42-43), and leaves are read straight from their unsliced
+// parent tensors: a sliced axis contributes `slice_stride` when its group's bit
+// of the global slice index is set (SlicedTensor.build, tensor.py:66-68).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define TOGB_MAXBITS 32
+
+struct OpDesc {
+  const void* ptr;        // device address of element (0,...,0) of slice 0
+  int64_t batch_stride;   // elements between consecutive slices in a chunk (0 for leaves)
+  int32_t outer_bits;     // log2 of the outer extent (M for A, N for B)
+  int32_t k_bits;         // log2 K
+  int32_t n_slice_terms;  // leaves: number of sliced axes
+  int32_t k_fast;         // loader hint: the operand's smallest stride lies on a k bit
+  int32_t leaf_shift;     // split mode, leaves: power-of-two normaliser
+  int32_t pad_;
+  int64_t s_outer[TOGB_MAXBITS];
+  int64_t s_k[TOGB_MAXBITS];
+  int64_t dk[TOGB_MAXBITS];            // dep_k(k+1) - dep_k(k) when bit t is the lowest zero of k
+  int32_t slice_shift[TOGB_MAXBITS];   // bit of the global slice index for sliced axis j
+  int64_t slice_stride[TOGB_MAXBITS];
+  const int32_t* exp_ptr;    // split mode, intermediates: per-slice exponent [chunk]
+  const uint32_t* max_ptr;   // split mode, intermediates: per-slice max bits [chunk]
+};
+
+struct JoinDesc {
+  OpDesc a, b;
+  int32_t mb, nb, kb;  // log2 M, N, K
+  int32_t join;        // index of this join in post-order
+  void* c_ptr;
+  int64_t c_batch_stride;
+  int64_t c_s_m[TOGB_MAXBITS];
+  int64_t c_s_n[TOGB_MAXBITS];
+  int32_t* c_exp;      // split mode: per-slice exponent of the output
+  uint32_t* c_max;     // split mode: per-slice max bits of the output (zeroed before the join)
+};
+
+// Root reduction: adds every slice's root tensor into the compensated FP64
+// accumulator, entry e of the result in the reference's axis order.
+struct RootDesc {
+  OpDesc r;            // outer bits = root entries in reference order
+  double* acc_sum;
+  double* acc_comp;
+};
+
+namespace togb {
+
+enum Kernel { K_DIRECT = 0, K_TILED = 1 };
+
+// Launchers (togb_kernels.cu).  `s0` points at the global index of the first
+// slice of the chunk; `nslices` is the number of slices in the chunk.
+cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t* s0, int nslices,
+                        cudaStream_t st);
+cudaError_t launch_root(int mode, const RootDesc& rd, const int64_t* s0, int nslices, cudaStream_t st);
+cudaError_t launch_set_s0(int64_t* d_s0, int64_t value, cudaStream_t st);
+cudaError_t probe_peak(int kind, cudaStream_t st, double* flops);
+
+}  // namespace togb

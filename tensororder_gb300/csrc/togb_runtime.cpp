@@ -1,0 +1,619 @@
+// Host runtime of the contraction path: lowers a flattened TensorOrder plan,
+// plans tensor layouts and a device arena, and queues the per-chunk kernel
+// sequence (optionally as a CUDA graph).  Implements include/togb.h.
+//
+// Lowering follows the reference's execution exactly:
+//  * the post-order stack walk of TensorNetwork.identify
+//    (src/tensor_network/tensor_network.pyx:142-156);
+//  * shared edges / output edge order of compute_join_properties
+//    (src/contraction_methods/contraction_tree.pyx:248-288): left unshared
+//    edges in order, then right unshared edges in order;
+//  * slicing by edge groups in itertools.product order
+//    (src/tensor_network/tensor_network.pyx:363-401), with every sliced axis
+//    removed from the tensors it touches (it is a size-1 axis in the
+//    reference, src/tensor_network/tensor.py:66-68);
+//  * the FP64 slice sum of BaseTensorAPI.contract_sliced
+//    (src/tensor_network/tensor_apis/base_api.py:21-28), done here with a
+//    compensated sum on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "togb.h"
+#include "togb_internal.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+togb_status fail(togb_status st, const std::string& msg) {
+  g_err = msg;
+  return st;
+}
+
+togb_status cuda_fail(cudaError_t e, const char* what) {
+  cudaGetLastError();
+  const togb_status st = (e == cudaErrorMemoryAllocation) ? TOGB_ERR_OOM : TOGB_ERR_CUDA;
+  return fail(st, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define TOGB_CUDA(x)                                  \
+  do {                                                \
+    cudaError_t e_ = (x);                             \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #x);  \
+  } while (0)
+
+constexpr int64_t kAlignElems = 32;  // arena offsets aligned to 32 elements
+
+struct Node {
+  int leaf = -1;                 // leaf index, or -1 for a join
+  int left = -1, right = -1;     // operand nodes of a join
+  int join = -1;                 // post-order index among joins
+  std::vector<int> ref;          // unsliced edges in the reference's axis order
+  std::unordered_map<int, int64_t> stride;  // unsliced edge -> element stride
+  int rank = 0;                  // number of unsliced axes
+  std::vector<int> m_lsb, n_lsb, k_lsb;     // GEMM bit order, least significant first
+  int64_t off = -1;              // per-slice arena offset (elements), joins only
+  int kernel = togb::K_DIRECT;
+};
+
+int64_t pow2(int r) { return int64_t(1) << r; }
+
+}  // namespace
+
+struct togb_program {
+  int device = 0;
+  int G = 0;
+  int64_t num_slices = 1;
+  std::vector<Node> nodes;
+  int root = -1;
+  std::vector<int> joins;  // node ids in execution (post-)order
+  std::unordered_map<int, int> group_of_edge;
+  // leaves
+  std::vector<int> leaf_rank;
+  std::vector<std::vector<int>> leaf_axes;
+  std::vector<int64_t> leaf_off;
+  std::vector<int> leaf_shift;  // split mode normaliser per leaf
+  double* d_leaf64 = nullptr;
+  float* d_leaf32 = nullptr;
+  // planning
+  int64_t arena = 0;  // per-slice elements
+  double flops = 0, bytes64 = 0;
+  int max_rank = 0;
+  // device state
+  double* d_acc = nullptr;  // [2 * 2^root_rank]: sum then compensation
+  int64_t* d_s0 = nullptr;
+  void* own_ws = nullptr;
+  size_t own_ws_bytes = 0;
+  cudaStream_t cap_stream = nullptr;
+  // descriptors for the current (mode, chunk, workspace)
+  int cur_mode = -1;
+  int cur_B = 0;
+  const void* cur_ws = nullptr;
+  std::vector<JoinDesc> jds;
+  RootDesc rd{};
+  uint32_t* d_max = nullptr;  // split mode max bits [joins][B] inside the workspace
+  size_t max_bytes = 0;
+  std::map<int, cudaGraphExec_t> graphs;  // by chunk slice count
+  bool use_graphs = true;
+  bool timing = false;
+  std::vector<float> join_ms;
+};
+
+namespace {
+
+size_t elem_size(int mode) { return mode == TOGB_MODE_F64 ? 8 : 4; }
+
+int64_t ws_per_slice(const togb_program* p, int mode) {
+  int64_t b = p->arena * (int64_t)elem_size(mode);
+  if (mode == TOGB_MODE_SPLIT) b += 8 * (int64_t)p->joins.size();  // exponent + max bits
+  return b;
+}
+
+const int64_t kWsFixed = 256;  // alignment slack
+
+void clear_graphs(togb_program* p) {
+  for (auto& kv : p->graphs) cudaGraphExecDestroy(kv.second);
+  p->graphs.clear();
+}
+
+// Choose the GEMM bit orders of a join and its output layout.
+void plan_join(togb_program* p, Node& J) {
+  const Node& L = p->nodes[J.left];
+  const Node& R = p->nodes[J.right];
+  std::vector<int> shared, lfree, rfree;
+  for (int e : L.ref) {
+    if (std::find(R.ref.begin(), R.ref.end(), e) != R.ref.end()) shared.push_back(e);
+    else lfree.push_back(e);
+  }
+  for (int e : R.ref)
+    if (std::find(L.ref.begin(), L.ref.end(), e) == L.ref.end()) rfree.push_back(e);
+  J.ref = lfree;
+  J.ref.insert(J.ref.end(), rfree.begin(), rfree.end());
+  J.rank = (int)J.ref.size();
+  auto by_stride = [](const Node& X) {
+    return [&X](int a, int b) { return X.stride.at(a) < X.stride.at(b); };
+  };
+  J.m_lsb = lfree;
+  std::sort(J.m_lsb.begin(), J.m_lsb.end(), by_stride(L));
+  J.n_lsb = rfree;
+  std::sort(J.n_lsb.begin(), J.n_lsb.end(), by_stride(R));
+  J.k_lsb = shared;
+  const Node& big = (L.rank >= R.rank) ? L : R;
+  std::sort(J.k_lsb.begin(), J.k_lsb.end(), by_stride(big));
+  // Output stored as C[m][n] row-major: n bits lowest.
+  const int nb = (int)J.n_lsb.size();
+  for (int i = 0; i < nb; ++i) J.stride[J.n_lsb[i]] = pow2(i);
+  for (size_t i = 0; i < J.m_lsb.size(); ++i) J.stride[J.m_lsb[i]] = pow2(nb + (int)i);
+  const int mb = (int)J.m_lsb.size(), kb = (int)J.k_lsb.size();
+  J.kernel = (mb >= 6 && nb >= 6 && kb >= 4) ? togb::K_TILED : togb::K_DIRECT;
+  const double M = std::ldexp(1.0, mb), N = std::ldexp(1.0, nb), K = std::ldexp(1.0, kb);
+  p->flops += 2.0 * M * N * K;
+  p->bytes64 += 8.0 * (M * K + K * N + M * N);
+}
+
+// First-fit arena over the join outputs, freeing operands after their consumer.
+void plan_arena(togb_program* p) {
+  std::vector<std::pair<int64_t, int64_t>> live;  // (offset, size), sorted by offset
+  int64_t top = 0;
+  auto alloc = [&](int64_t size) {
+    int64_t cur = 0;
+    size_t pos = 0;
+    for (; pos < live.size(); ++pos) {
+      if (live[pos].first - cur >= size) break;
+      cur = live[pos].first + live[pos].second;
+    }
+    live.insert(live.begin() + pos, {cur, size});
+    top = std::max(top, cur + size);
+    return cur;
+  };
+  auto release = [&](int64_t off) {
+    for (size_t i = 0; i < live.size(); ++i)
+      if (live[i].first == off) { live.erase(live.begin() + i); return; }
+  };
+  for (int id : p->joins) {
+    Node& J = p->nodes[id];
+    const int64_t size = (pow2(J.rank) + kAlignElems - 1) / kAlignElems * kAlignElems;
+    J.off = alloc(size);
+    for (int opnd : {J.left, J.right})
+      if (p->nodes[opnd].leaf < 0) release(p->nodes[opnd].off);
+  }
+  p->arena = std::max<int64_t>(top, kAlignElems);
+}
+
+void fill_operand(const togb_program* p, const Node& X, const std::vector<int>& outer,
+                  const std::vector<int>& k, int mode, char* ws, int B, OpDesc& od) {
+  std::memset(&od, 0, sizeof(od));
+  const size_t es = elem_size(mode);
+  if (X.leaf >= 0) {
+    const char* base = mode == TOGB_MODE_F64 ? (const char*)p->d_leaf64 : (const char*)p->d_leaf32;
+    od.ptr = base + p->leaf_off[X.leaf] * es;
+    od.batch_stride = 0;
+    const std::vector<int>& axes = p->leaf_axes[X.leaf];
+    const int R = (int)axes.size();
+    int nt = 0;
+    for (int a = 0; a < R; ++a) {
+      auto it = p->group_of_edge.find(axes[a]);
+      if (it == p->group_of_edge.end()) continue;
+      od.slice_shift[nt] = p->G - 1 - it->second;
+      od.slice_stride[nt] = pow2(R - 1 - a);
+      ++nt;
+    }
+    od.n_slice_terms = nt;
+    od.leaf_shift = p->leaf_shift[X.leaf];
+  } else {
+    od.ptr = ws + X.off * (int64_t)B * es;
+    od.batch_stride = pow2(X.rank);
+    if (mode == TOGB_MODE_SPLIT) {
+      char* meta = ws + p->arena * (int64_t)B * es;
+      od.exp_ptr = (const int32_t*)(meta) + (int64_t)X.join * B;
+      od.max_ptr = (const uint32_t*)(meta + 4 * (int64_t)p->joins.size() * B) + (int64_t)X.join * B;
+    }
+  }
+  od.outer_bits = (int)outer.size();
+  od.k_bits = (int)k.size();
+  int64_t min_outer = INT64_MAX, min_k = INT64_MAX;
+  for (size_t i = 0; i < outer.size(); ++i) {
+    od.s_outer[i] = X.stride.at(outer[i]);
+    min_outer = std::min(min_outer, od.s_outer[i]);
+  }
+  int64_t prefix = 0;
+  for (size_t i = 0; i < k.size(); ++i) {
+    od.s_k[i] = X.stride.at(k[i]);
+    min_k = std::min(min_k, od.s_k[i]);
+    od.dk[i] = od.s_k[i] - prefix;
+    prefix += od.s_k[i];
+  }
+  od.k_fast = min_k < min_outer ? 1 : 0;
+}
+
+void build_descs(togb_program* p, int mode, void* ws_v, int B) {
+  char* ws = (char*)ws_v;
+  const size_t es = elem_size(mode);
+  p->jds.assign(p->joins.size(), JoinDesc{});
+  for (size_t j = 0; j < p->joins.size(); ++j) {
+    const Node& J = p->nodes[p->joins[j]];
+    JoinDesc& jd = p->jds[j];
+    std::memset(&jd, 0, sizeof(jd));
+    fill_operand(p, p->nodes[J.left], J.m_lsb, J.k_lsb, mode, ws, B, jd.a);
+    fill_operand(p, p->nodes[J.right], J.n_lsb, J.k_lsb, mode, ws, B, jd.b);
+    jd.mb = (int)J.m_lsb.size();
+    jd.nb = (int)J.n_lsb.size();
+    jd.kb = (int)J.k_lsb.size();
+    jd.join = (int)j;
+    jd.c_ptr = ws + J.off * (int64_t)B * es;
+    jd.c_batch_stride = pow2(J.rank);
+    for (int i = 0; i < jd.mb; ++i) jd.c_s_m[i] = J.stride.at(J.m_lsb[i]);
+    for (int i = 0; i < jd.nb; ++i) jd.c_s_n[i] = J.stride.at(J.n_lsb[i]);
+    if (mode == TOGB_MODE_SPLIT) {
+      char* meta = ws + p->arena * (int64_t)B * es;
+      jd.c_exp = (int32_t*)meta + (int64_t)j * B;
+      jd.c_max = (uint32_t*)(meta + 4 * (int64_t)p->joins.size() * B) + (int64_t)j * B;
+    }
+  }
+  // Root: outer bits enumerate the reference axis order, last axis lowest.
+  const Node& Rn = p->nodes[p->root];
+  std::vector<int> ref_lsb(Rn.ref.rbegin(), Rn.ref.rend());
+  fill_operand(p, Rn, ref_lsb, {}, mode, ws, B, p->rd.r);
+  p->rd.acc_sum = p->d_acc;
+  p->rd.acc_comp = p->d_acc + pow2(Rn.rank);
+  if (mode == TOGB_MODE_SPLIT) {
+    p->d_max = (uint32_t*)(ws + p->arena * (int64_t)B * es + 4 * (int64_t)p->joins.size() * B);
+    p->max_bytes = 4 * p->joins.size() * (size_t)B;
+  } else {
+    p->d_max = nullptr;
+    p->max_bytes = 0;
+  }
+}
+
+togb_status enqueue_chunk(togb_program* p, int mode, int nb, cudaStream_t st,
+                          std::vector<cudaEvent_t>* ev) {
+  // Split mode: every output's per-slice maximum starts at +0 (atomicMax target).
+  if (p->max_bytes) TOGB_CUDA(cudaMemsetAsync(p->d_max, 0, p->max_bytes, st));
+  for (size_t j = 0; j < p->joins.size(); ++j) {
+    if (ev) TOGB_CUDA(cudaEventRecord((*ev)[j], st));
+    const Node& J = p->nodes[p->joins[j]];
+    cudaError_t e = togb::launch_join(mode, J.kernel, p->jds[j], p->d_s0, nb, st);
+    if (e != cudaSuccess) return cuda_fail(e, "join kernel launch");
+  }
+  if (ev) TOGB_CUDA(cudaEventRecord((*ev)[p->joins.size()], st));
+  cudaError_t e = togb::launch_root(mode, p->rd, p->d_s0, nb, st);
+  if (e != cudaSuccess) return cuda_fail(e, "root kernel launch");
+  return TOGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int togb_version(void) { return 1; }
+
+const char* togb_last_error(void) { return g_err.c_str(); }
+
+togb_status togb_program_create(const togb_program_desc* d, int device, togb_program** out) {
+  if (!d || !out) return fail(TOGB_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (d->num_leaves <= 0 || d->num_tokens <= 0) return fail(TOGB_ERR_INVALID, "empty program");
+  if (d->num_groups < 0 || d->num_groups > 40) return fail(TOGB_ERR_UNSUPPORTED, "at most 40 slice groups");
+  togb_program* p = new togb_program();
+  p->device = device;
+  p->G = d->num_groups;
+  p->num_slices = pow2(p->G);
+  // Slice groups.
+  int64_t ge = 0;
+  for (int g = 0; g < d->num_groups; ++g) {
+    if (d->group_size[g] <= 0) { delete p; return fail(TOGB_ERR_INVALID, "empty slice group"); }
+    for (int i = 0; i < d->group_size[g]; ++i) {
+      const int e = d->group_edges[ge++];
+      if (!p->group_of_edge.emplace(e, g).second) {
+        delete p;
+        return fail(TOGB_ERR_INVALID, "edge listed in two slice groups");
+      }
+    }
+  }
+  // Leaves.
+  p->leaf_rank.assign(d->leaf_rank, d->leaf_rank + d->num_leaves);
+  p->leaf_axes.resize(d->num_leaves);
+  p->leaf_off.resize(d->num_leaves);
+  p->leaf_shift.resize(d->num_leaves);
+  int64_t ax = 0, voff = 0;
+  for (int l = 0; l < d->num_leaves; ++l) {
+    const int r = d->leaf_rank[l];
+    if (r < 0 || r > 30) { delete p; return fail(TOGB_ERR_UNSUPPORTED, "leaf rank outside [0, 30]"); }
+    p->leaf_axes[l].assign(d->leaf_axes + ax, d->leaf_axes + ax + r);
+    ax += r;
+    p->leaf_off[l] = voff;
+    double mx = 0;
+    for (int64_t i = 0; i < pow2(r); ++i) {
+      const double v = d->leaf_values[voff + i];
+      if (!(v >= 0) || std::isinf(v)) {
+        delete p;
+        return fail(TOGB_ERR_UNSUPPORTED, "leaf entries must be finite and non-negative");
+      }
+      mx = std::max(mx, v);
+    }
+    int e2 = 0;
+    if (mx > 0) std::frexp(mx, &e2);  // mx in [2^(e2-1), 2^e2)
+    p->leaf_shift[l] = mx > 0 ? 1 - e2 : 0;
+    voff += pow2(r);
+  }
+  // Post-order walk (TensorNetwork.identify).
+  std::vector<int> stack;
+  std::vector<char> used(d->num_leaves, 0);
+  for (int t = 0; t < d->num_tokens; ++t) {
+    const int tok = d->postorder[t];
+    if (tok >= 0) {
+      if (tok >= d->num_leaves || used[tok]) { delete p; return fail(TOGB_ERR_INVALID, "bad leaf token"); }
+      used[tok] = 1;
+      Node n;
+      n.leaf = tok;
+      const std::vector<int>& axes = p->leaf_axes[tok];
+      const int R = (int)axes.size();
+      for (int a = 0; a < R; ++a) {
+        if (p->group_of_edge.count(axes[a])) continue;
+        if (n.stride.count(axes[a])) { delete p; return fail(TOGB_ERR_INVALID, "repeated edge in a leaf"); }
+        n.ref.push_back(axes[a]);
+        n.stride[axes[a]] = pow2(R - 1 - a);
+      }
+      n.rank = (int)n.ref.size();
+      p->nodes.push_back(std::move(n));
+      stack.push_back((int)p->nodes.size() - 1);
+    } else {
+      if (stack.size() < 2) { delete p; return fail(TOGB_ERR_INVALID, "join without two operands"); }
+      Node n;
+      n.right = stack.back(); stack.pop_back();
+      n.left = stack.back(); stack.pop_back();
+      n.join = (int)p->joins.size();
+      p->nodes.push_back(std::move(n));
+      const int id = (int)p->nodes.size() - 1;
+      plan_join(p, p->nodes[id]);
+      if (p->nodes[id].rank > 30) { delete p; return fail(TOGB_ERR_UNSUPPORTED, "intermediate rank above 30"); }
+      p->joins.push_back(id);
+      stack.push_back(id);
+    }
+  }
+  if (stack.size() != 1) { delete p; return fail(TOGB_ERR_INVALID, "post-order does not reduce to one tensor"); }
+  for (int l = 0; l < d->num_leaves; ++l)
+    if (!used[l]) { delete p; return fail(TOGB_ERR_INVALID, "leaf never pushed"); }
+  p->root = stack[0];
+  for (const Node& n : p->nodes) p->max_rank = std::max(p->max_rank, n.rank);
+  plan_arena(p);
+
+  // Device side.
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) { delete p; return cuda_fail(e, "cudaSetDevice"); }
+  std::vector<float> v32(voff);
+  for (int64_t i = 0; i < voff; ++i) v32[i] = (float)d->leaf_values[i];
+  const int64_t E = pow2(p->nodes[p->root].rank);
+  if ((e = cudaMalloc(&p->d_leaf64, std::max<int64_t>(voff, 1) * 8)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_leaf32, std::max<int64_t>(voff, 1) * 4)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_acc, 2 * E * 8)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_s0, 8)) != cudaSuccess ||
+      (e = cudaMemcpy(p->d_leaf64, d->leaf_values, voff * 8, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(p->d_leaf32, v32.data(), voff * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemset(p->d_acc, 0, 2 * E * 8)) != cudaSuccess ||
+      (e = cudaMemset(p->d_s0, 0, 8)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    togb_program_destroy(p);
+    return cuda_fail(e, "program allocation");
+  }
+  *out = p;
+  return TOGB_OK;
+}
+
+togb_status togb_program_info_get(const togb_program* p, togb_program_info* info) {
+  if (!p || !info) return fail(TOGB_ERR_INVALID, "null argument");
+  info->num_slices = p->num_slices;
+  info->num_joins = (int32_t)p->joins.size();
+  info->max_rank = p->max_rank;
+  info->root_rank = p->nodes[p->root].rank;
+  info->num_launches = (int32_t)p->joins.size() + 1;
+  info->flops_per_slice = p->flops;
+  info->bytes_per_slice_f64 = p->bytes64;
+  for (int m = 0; m < 2; ++m) {
+    info->workspace_per_slice[m] = ws_per_slice(p, m);
+    info->workspace_fixed[m] = kWsFixed;
+  }
+  return TOGB_OK;
+}
+
+togb_status togb_program_reset(togb_program* p, void* stream) {
+  if (!p) return fail(TOGB_ERR_INVALID, "null program");
+  TOGB_CUDA(cudaSetDevice(p->device));
+  const int64_t E = pow2(p->nodes[p->root].rank);
+  TOGB_CUDA(cudaMemsetAsync(p->d_acc, 0, 2 * E * 8, (cudaStream_t)stream));
+  return TOGB_OK;
+}
+
+togb_status togb_program_set_timing(togb_program* p, int enable) {
+  if (!p) return fail(TOGB_ERR_INVALID, "null program");
+  p->timing = enable != 0;
+  return TOGB_OK;
+}
+
+togb_status togb_program_join_times(togb_program* p, float* ms, int32_t n) {
+  if (!p || !ms) return fail(TOGB_ERR_INVALID, "null argument");
+  if (n != (int32_t)p->joins.size() || p->join_ms.size() != p->joins.size())
+    return fail(TOGB_ERR_INVALID, "no timing recorded for this program (enable timing, then run)");
+  std::copy(p->join_ms.begin(), p->join_ms.end(), ms);
+  return TOGB_OK;
+}
+
+togb_status togb_program_run(togb_program* p, int mode, int64_t begin, int64_t end, void* workspace,
+                             size_t ws_bytes, void* stream_v) {
+  if (!p) return fail(TOGB_ERR_INVALID, "null program");
+  if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
+  if (begin < 0 || end > p->num_slices || begin > end) return fail(TOGB_ERR_INVALID, "slice range out of bounds");
+  if (begin == end) return TOGB_OK;
+  cudaStream_t st = (cudaStream_t)stream_v;
+  TOGB_CUDA(cudaSetDevice(p->device));
+  const int64_t per = ws_per_slice(p, mode);
+  const int64_t want = end - begin;
+  if (!workspace) {
+    // Own workspace: as many slices per chunk as fit a quarter of free memory.
+    size_t freeb = 0, totalb = 0;
+    TOGB_CUDA(cudaMemGetInfo(&freeb, &totalb));
+    int64_t fit = (int64_t)(freeb / 4 + p->own_ws_bytes) / per;
+    int64_t B = std::max<int64_t>(1, std::min<int64_t>(want, std::min<int64_t>(fit, 65535)));
+    const size_t need = (size_t)(B * per + kWsFixed);
+    if (p->own_ws_bytes < need) {
+      if (p->own_ws) { cudaFree(p->own_ws); p->own_ws = nullptr; p->own_ws_bytes = 0; }
+      cudaError_t e = cudaMalloc(&p->own_ws, need);
+      if (e != cudaSuccess) return cuda_fail(e, "workspace allocation");
+      p->own_ws_bytes = need;
+    }
+    workspace = p->own_ws;
+    ws_bytes = p->own_ws_bytes;
+  }
+  char* ws = (char*)(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+  const int64_t usable = (int64_t)ws_bytes - (int64_t)(ws - (char*)workspace);
+  int64_t B = usable > 0 ? usable / per : 0;
+  B = std::min<int64_t>(B, std::min<int64_t>(want, 65535));
+  if (B < 1) return fail(TOGB_ERR_OOM, "workspace smaller than one slice");
+  if (mode != p->cur_mode || B != p->cur_B || ws != p->cur_ws) {
+    clear_graphs(p);
+    build_descs(p, mode, ws, (int)B);
+    p->cur_mode = mode;
+    p->cur_B = (int)B;
+    p->cur_ws = ws;
+  }
+  std::vector<cudaEvent_t> ev;
+  if (p->timing) {
+    ev.resize(p->joins.size() + 1);
+    for (auto& x : ev) TOGB_CUDA(cudaEventCreate(&x));
+    p->join_ms.assign(p->joins.size(), 0.f);
+  }
+  for (int64_t s = begin; s < end; s += B) {
+    const int nb = (int)std::min<int64_t>(B, end - s);
+    cudaError_t e = togb::launch_set_s0(p->d_s0, s, st);
+    if (e != cudaSuccess) return cuda_fail(e, "slice base update");
+    if (p->timing || !p->use_graphs) {
+      togb_status r = enqueue_chunk(p, mode, nb, st, p->timing ? &ev : nullptr);
+      if (r != TOGB_OK) return r;
+      if (p->timing) {
+        TOGB_CUDA(cudaEventSynchronize(ev.back()));
+        for (size_t j = 0; j < p->joins.size(); ++j) {
+          float ms = 0;
+          TOGB_CUDA(cudaEventElapsedTime(&ms, ev[j], ev[j + 1]));
+          p->join_ms[j] += ms;
+        }
+      }
+      continue;
+    }
+    auto it = p->graphs.find(nb);
+    if (it == p->graphs.end()) {
+      cudaGraph_t g = nullptr;
+      TOGB_CUDA(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
+      togb_status r = enqueue_chunk(p, mode, nb, p->cap_stream, nullptr);
+      cudaError_t ce = cudaStreamEndCapture(p->cap_stream, &g);
+      if (r != TOGB_OK) { if (g) cudaGraphDestroy(g); return r; }
+      if (ce != cudaSuccess) return cuda_fail(ce, "graph capture");
+      cudaGraphExec_t ex = nullptr;
+      ce = cudaGraphInstantiate(&ex, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) return cuda_fail(ce, "graph instantiate");
+      it = p->graphs.emplace(nb, ex).first;
+    }
+    TOGB_CUDA(cudaGraphLaunch(it->second, st));
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  return TOGB_OK;
+}
+
+togb_status togb_program_result(togb_program* p, void* stream, double* out, double* comp, int64_t n) {
+  if (!p || !out) return fail(TOGB_ERR_INVALID, "null argument");
+  const int64_t E = pow2(p->nodes[p->root].rank);
+  if (n != E) return fail(TOGB_ERR_INVALID, "result size does not match the root tensor");
+  TOGB_CUDA(cudaSetDevice(p->device));
+  TOGB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  std::vector<double> h(2 * E);
+  TOGB_CUDA(cudaMemcpy(h.data(), p->d_acc, 2 * E * 8, cudaMemcpyDeviceToHost));
+  for (int64_t i = 0; i < E; ++i) {
+    out[i] = h[i] + h[E + i];
+    if (comp) comp[i] = h[E + i];
+  }
+  return TOGB_OK;
+}
+
+void togb_program_destroy(togb_program* p) {
+  if (!p) return;
+  cudaSetDevice(p->device);
+  clear_graphs(p);
+  cudaFree(p->d_leaf64);
+  cudaFree(p->d_leaf32);
+  cudaFree(p->d_acc);
+  cudaFree(p->d_s0);
+  if (p->own_ws) cudaFree(p->own_ws);
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+  delete p;
+}
+
+togb_status togb_tensordot_f64(const double* a, int32_t ra, const double* b, int32_t rb, int32_t n_axes,
+                               const int32_t* axes_a, const int32_t* axes_b, double* out, void* stream) {
+  if (!a || !b || !out) return fail(TOGB_ERR_INVALID, "null tensor");
+  if (ra < 0 || rb < 0 || ra > 30 || rb > 30 || n_axes < 0 || n_axes > std::min(ra, rb))
+    return fail(TOGB_ERR_INVALID, "bad ranks or axis count");
+  std::vector<char> in_a(ra, 0), in_b(rb, 0);
+  for (int i = 0; i < n_axes; ++i) {
+    if (axes_a[i] < 0 || axes_a[i] >= ra || axes_b[i] < 0 || axes_b[i] >= rb || in_a[axes_a[i]] || in_b[axes_b[i]])
+      return fail(TOGB_ERR_INVALID, "bad contraction axes");
+    in_a[axes_a[i]] = 1;
+    in_b[axes_b[i]] = 1;
+  }
+  if (ra + rb - 2 * n_axes > 30) return fail(TOGB_ERR_UNSUPPORTED, "output rank above 30");
+  JoinDesc jd;
+  std::memset(&jd, 0, sizeof(jd));
+  std::vector<int> afree, bfree;
+  for (int i = 0; i < ra; ++i) if (!in_a[i]) afree.push_back(i);
+  for (int i = 0; i < rb; ++i) if (!in_b[i]) bfree.push_back(i);
+  jd.mb = (int)afree.size();
+  jd.nb = (int)bfree.size();
+  jd.kb = n_axes;
+  // LSB-first: the last free axis of each operand is the lowest GEMM bit, so
+  // C[m][n] row-major is np.tensordot's output order.
+  for (int i = 0; i < jd.mb; ++i) jd.a.s_outer[i] = pow2(ra - 1 - afree[jd.mb - 1 - i]);
+  for (int i = 0; i < jd.nb; ++i) jd.b.s_outer[i] = pow2(rb - 1 - bfree[jd.nb - 1 - i]);
+  int64_t pa = 0, pb = 0, mina = INT64_MAX, minb = INT64_MAX, mino_a = INT64_MAX, mino_b = INT64_MAX;
+  for (int i = 0; i < n_axes; ++i) {
+    const int src = n_axes - 1 - i;
+    jd.a.s_k[i] = pow2(ra - 1 - axes_a[src]);
+    jd.b.s_k[i] = pow2(rb - 1 - axes_b[src]);
+    jd.a.dk[i] = jd.a.s_k[i] - pa; pa += jd.a.s_k[i];
+    jd.b.dk[i] = jd.b.s_k[i] - pb; pb += jd.b.s_k[i];
+    mina = std::min(mina, jd.a.s_k[i]);
+    minb = std::min(minb, jd.b.s_k[i]);
+  }
+  for (int i = 0; i < jd.mb; ++i) mino_a = std::min(mino_a, jd.a.s_outer[i]);
+  for (int i = 0; i < jd.nb; ++i) mino_b = std::min(mino_b, jd.b.s_outer[i]);
+  jd.a.k_fast = mina < mino_a;
+  jd.b.k_fast = minb < mino_b;
+  jd.a.ptr = a;
+  jd.b.ptr = b;
+  jd.a.outer_bits = jd.mb; jd.a.k_bits = jd.kb;
+  jd.b.outer_bits = jd.nb; jd.b.k_bits = jd.kb;
+  jd.a.batch_stride = pow2(ra);
+  jd.b.batch_stride = pow2(rb);
+  jd.c_ptr = out;
+  jd.c_batch_stride = pow2(jd.mb + jd.nb);
+  for (int i = 0; i < jd.nb; ++i) jd.c_s_n[i] = pow2(i);
+  for (int i = 0; i < jd.mb; ++i) jd.c_s_m[i] = pow2(jd.nb + i);
+  const int kernel = (jd.mb >= 6 && jd.nb >= 6 && jd.kb >= 4) ? togb::K_TILED : togb::K_DIRECT;
+  cudaError_t e = togb::launch_join(TOGB_MODE_F64, kernel, jd, nullptr, 1, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "tensordot launch");
+  return TOGB_OK;
+}
+
+togb_status togb_probe_peak(int kind, void* stream, double* flops) {
+  if (!flops || (kind != 0 && kind != 1)) return fail(TOGB_ERR_INVALID, "bad probe arguments");
+  cudaError_t e = togb::probe_peak(kind, (cudaStream_t)stream, flops);
+  if (e != cudaSuccess) return cuda_fail(e, "peak probe");
+  return TOGB_OK;
+}
+
+}  // extern "C"

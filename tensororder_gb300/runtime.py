@@ -1,0 +1,251 @@
+"""ctypes bindings of ``libtogb.so`` (the C ABI declared in ``include/togb.h``).
+
+PyTorch is used only for device memory and streams: workspaces are
+``torch.empty(..., dtype=torch.uint8, device="cuda")`` buffers and work is
+queued on ``torch.cuda.current_stream()``.  No compute goes through torch.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+from .program import Program
+
+MODE_F64 = 0
+MODE_SPLIT = 1
+
+OK, ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_UNSUPPORTED, ERR_TIMEOUT = range(6)
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+class ProgramDesc(ctypes.Structure):
+    _fields_ = [
+        ("num_leaves", ctypes.c_int32),
+        ("leaf_rank", _i32p),
+        ("leaf_axes", _i32p),
+        ("leaf_values", _f64p),
+        ("num_tokens", ctypes.c_int32),
+        ("postorder", _i32p),
+        ("num_groups", ctypes.c_int32),
+        ("group_size", _i32p),
+        ("group_edges", _i32p),
+    ]
+
+
+class ProgramInfo(ctypes.Structure):
+    _fields_ = [
+        ("num_slices", ctypes.c_int64),
+        ("num_joins", ctypes.c_int32),
+        ("max_rank", ctypes.c_int32),
+        ("root_rank", ctypes.c_int32),
+        ("num_launches", ctypes.c_int32),
+        ("flops_per_slice", ctypes.c_double),
+        ("bytes_per_slice_f64", ctypes.c_double),
+        ("workspace_per_slice", ctypes.c_int64 * 2),
+        ("workspace_fixed", ctypes.c_int64 * 2),
+    ]
+
+
+class TogbError(RuntimeError):
+    """A failed call into libtogb; ``status`` is the togb_status code."""
+
+    def __init__(self, status, message):
+        super().__init__("libtogb status %d: %s" % (status, message))
+        self.status = status
+
+
+class DeviceOutOfMemory(TogbError):
+    """Device memory did not suffice (TOGB_ERR_OOM or a failed torch allocation)."""
+
+
+_lib = None
+
+EXPORTS = [
+    "togb_version", "togb_last_error", "togb_program_create", "togb_program_info_get",
+    "togb_program_reset", "togb_program_run", "togb_program_result", "togb_program_set_timing",
+    "togb_program_join_times", "togb_program_destroy", "togb_tensordot_f64", "togb_probe_peak",
+]
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib():
+    """Load ``libtogb.so``; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError("libtogb.so is missing (%s); run tensororder_gb300.build.build()" % path)
+    L = ctypes.CDLL(path)
+    c_void = ctypes.c_void_p
+    L.togb_version.restype = ctypes.c_int
+    L.togb_last_error.restype = ctypes.c_char_p
+    L.togb_program_create.argtypes = [ctypes.POINTER(ProgramDesc), ctypes.c_int, ctypes.POINTER(c_void)]
+    L.togb_program_info_get.argtypes = [c_void, ctypes.POINTER(ProgramInfo)]
+    L.togb_program_reset.argtypes = [c_void, c_void]
+    L.togb_program_run.argtypes = [c_void, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, c_void, ctypes.c_size_t, c_void]
+    L.togb_program_result.argtypes = [c_void, c_void, _f64p, _f64p, ctypes.c_int64]
+    L.togb_program_set_timing.argtypes = [c_void, ctypes.c_int]
+    L.togb_program_join_times.argtypes = [c_void, ctypes.POINTER(ctypes.c_float), ctypes.c_int32]
+    L.togb_program_destroy.argtypes = [c_void]
+    L.togb_program_destroy.restype = None
+    L.togb_tensordot_f64.argtypes = [c_void, ctypes.c_int32, c_void, ctypes.c_int32, ctypes.c_int32,
+                                     _i32p, _i32p, c_void, c_void]
+    L.togb_probe_peak.argtypes = [ctypes.c_int, c_void, ctypes.POINTER(ctypes.c_double)]
+    for name in EXPORTS:
+        if name not in ("togb_version", "togb_last_error", "togb_program_destroy"):
+            getattr(L, name).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != OK:
+        msg = lib().togb_last_error().decode(errors="replace")
+        if status == ERR_OOM:
+            raise DeviceOutOfMemory(status, msg)
+        raise TogbError(status, msg)
+
+
+def _stream_handle(stream):
+    import torch
+
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+class DeviceProgram:
+    """A program lowered and planned by libtogb, with its leaves on the device."""
+
+    def __init__(self, program: Program, device: int = 0):
+        self.program = program
+        self.device = device
+        leaves = program.leaves
+        self._ranks = np.array([l.rank for l in leaves], dtype=np.int32)
+        self._axes = np.array([a for l in leaves for a in l.axes] or [0], dtype=np.int32)
+        vals = [l.parent().ravel() for l in leaves]
+        self._values = np.ascontiguousarray(np.concatenate(vals) if vals else np.zeros(1), dtype=np.float64)
+        self._tokens = np.array(program.postorder, dtype=np.int32)
+        self._gsize = np.array([len(g) for g in program.slice_groups] or [0], dtype=np.int32)
+        self._gedges = np.array([e for g in program.slice_groups for e in g] or [0], dtype=np.int32)
+        desc = ProgramDesc(
+            len(leaves), self._ranks.ctypes.data_as(_i32p), self._axes.ctypes.data_as(_i32p),
+            self._values.ctypes.data_as(_f64p), len(self._tokens), self._tokens.ctypes.data_as(_i32p),
+            len(program.slice_groups), self._gsize.ctypes.data_as(_i32p), self._gedges.ctypes.data_as(_i32p),
+        )
+        handle = ctypes.c_void_p()
+        check(lib().togb_program_create(ctypes.byref(desc), device, ctypes.byref(handle)))
+        self._h = handle
+        info = ProgramInfo()
+        check(lib().togb_program_info_get(self._h, ctypes.byref(info)))
+        self.info = info
+        self._workspace = None
+
+    @property
+    def num_slices(self):
+        return int(self.info.num_slices)
+
+    def workspace_bytes(self, mode, slices):
+        return int(self.info.workspace_per_slice[mode]) * int(slices) + int(self.info.workspace_fixed[mode])
+
+    def allocate_workspace(self, mode, slices, max_fraction=0.5):
+        """A torch uint8 device buffer for up to ``slices`` slices per chunk,
+        capped at ``max_fraction`` of free device memory (at least one slice)."""
+        import torch
+
+        per = int(self.info.workspace_per_slice[mode])
+        free, _ = torch.cuda.mem_get_info(self.device)
+        cap = max(1, int(free * max_fraction) // max(per, 1))
+        n = max(1, min(int(slices), cap))
+        want = self.workspace_bytes(mode, n)
+        if self._workspace is not None and self._workspace.numel() >= want:
+            return self._workspace
+        self._workspace = None
+        try:
+            self._workspace = torch.empty(want, dtype=torch.uint8, device="cuda:%d" % self.device)
+        except torch.cuda.OutOfMemoryError as e:
+            raise DeviceOutOfMemory(ERR_OOM, str(e))
+        return self._workspace
+
+    def reset(self, stream=None):
+        check(lib().togb_program_reset(self._h, _stream_handle(stream)))
+
+    def run(self, mode, begin=0, end=None, workspace=None, stream=None):
+        end = self.num_slices if end is None else end
+        if workspace is None:
+            ptr, nbytes = None, 0
+        else:
+            ptr, nbytes = workspace.data_ptr(), workspace.numel() * workspace.element_size()
+        check(lib().togb_program_run(self._h, int(mode), int(begin), int(end), ctypes.c_void_p(ptr),
+                                     ctypes.c_size_t(nbytes), _stream_handle(stream)))
+
+    def result(self, stream=None):
+        n = 1 << int(self.info.root_rank)
+        out = np.zeros(n, dtype=np.float64)
+        check(lib().togb_program_result(self._h, _stream_handle(stream), out.ctypes.data_as(_f64p), None, n))
+        return out.reshape((2,) * int(self.info.root_rank))
+
+    def set_timing(self, enable=True):
+        check(lib().togb_program_set_timing(self._h, 1 if enable else 0))
+
+    def join_times(self):
+        n = int(self.info.num_joins)
+        out = (ctypes.c_float * n)()
+        check(lib().togb_program_join_times(self._h, out, n))
+        return np.array(out, dtype=np.float64)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().togb_program_destroy(self._h)
+            self._h = None
+        self._workspace = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tensordot_f64(a, b, axes, out=None, stream=None):
+    """``np.tensordot(a, b, axes)`` for binary-index FP64 CUDA tensors (torch)."""
+    import torch
+
+    axes_a, axes_b = [list(x) for x in axes]
+    if len(axes_a) != len(axes_b):
+        raise ValueError("shape-mismatch for sum")
+    for t in (a, b):
+        if t.dtype != torch.float64 or not t.is_cuda:
+            raise TypeError("tensordot_f64 takes float64 CUDA tensors")
+        if any(d != 2 for d in t.shape):
+            raise ValueError("only binary (dimension-2) indices are supported")
+    ra, rb = a.dim(), b.dim()
+    axes_a = [x % ra if ra else x for x in axes_a]
+    axes_b = [x % rb if rb else x for x in axes_b]
+    a = a.contiguous()
+    b = b.contiguous()
+    rank = ra + rb - 2 * len(axes_a)
+    if out is None:
+        out = torch.empty((2,) * rank, dtype=torch.float64, device=a.device)
+    aa = np.array(axes_a or [0], dtype=np.int32)
+    bb = np.array(axes_b or [0], dtype=np.int32)
+    check(lib().togb_tensordot_f64(ctypes.c_void_p(a.data_ptr()), ra, ctypes.c_void_p(b.data_ptr()), rb,
+                                   len(axes_a), aa.ctypes.data_as(_i32p), bb.ctypes.data_as(_i32p),
+                                   ctypes.c_void_p(out.data_ptr()), _stream_handle(stream)))
+    return out
+
+
+def probe_peak(kind, stream=None):
+    """Measured FMA throughput in FLOP/s: kind 0 = FP64, 1 = FP32."""
+    v = ctypes.c_double()
+    check(lib().togb_probe_peak(int(kind), _stream_handle(stream), ctypes.byref(v)))
+    return v.value
