@@ -20,6 +20,16 @@
 
 #define TOGB_MAXBITS 32
 
+// A deposit as bit-field moves: every stride is a power of two, so
+// dep(x) = sum_r ((x >> src[r]) & (2^len[r] - 1)) << dst[r] over maximal runs of
+// consecutive index bits that land on consecutive address bits.
+struct Runs {
+  int32_t n;
+  int8_t src[TOGB_MAXBITS];
+  int8_t len[TOGB_MAXBITS];
+  int8_t dst[TOGB_MAXBITS];
+};
+
 struct OpDesc {
   const void* ptr;        // device address of element (0,...,0) of slice 0
   int64_t batch_stride;   // elements between consecutive slices in a chunk (0 for leaves)
@@ -36,6 +46,9 @@ struct OpDesc {
   int64_t slice_stride[TOGB_MAXBITS];
   const int32_t* exp_ptr;    // split mode, intermediates: per-slice exponent [chunk]
   const uint32_t* max_ptr;   // split mode, intermediates: per-slice max bits [chunk]
+  const void* ptr_lo;        // split mode, leaves: FP32 residual (value - hi), same layout
+  Runs r_outer;              // run form of s_outer
+  Runs r_k;                  // run form of s_k
 };
 
 struct JoinDesc {
@@ -48,6 +61,7 @@ struct JoinDesc {
   int64_t c_s_n[TOGB_MAXBITS];
   int32_t* c_exp;      // split mode: per-slice exponent of the output
   uint32_t* c_max;     // split mode: per-slice max bits of the output (zeroed before the join)
+  Runs r_cm, r_cn;     // run forms of c_s_m / c_s_n
 };
 
 // Root reduction: adds every slice's root tensor into the compensated FP64
@@ -60,7 +74,10 @@ struct RootDesc {
 
 namespace togb {
 
-enum Kernel { K_DIRECT = 0, K_TILED = 1 };
+enum Kernel { K_DIRECT = 0, K_TILED = 1, K_REDUCE = 2 };
+
+// Host helper: run form of a stride table (strides must be powers of two).
+void make_runs(const int64_t* s, int nbits, Runs* out);
 
 // Launchers (togb_kernels.cu).  `s0` points at the global index of the first
 // slice of the chunk; `nslices` is the number of slices in the chunk.

@@ -8,6 +8,10 @@
 //  * k_tiled  -- 64x64x16 shared-memory tiled GEMM, 4x4 register blocking.
 //    Tiles are gathered through per-CTA offset tables, so any axis
 //    permutation of either operand is read in place (no transpose pass).
+//  * k_reduce -- one CTA per (slice, output entry) for joins with a few
+//    outputs and a long K (the root of a tree is a 1x1xK dot product): strided
+//    per-thread partial sums (compensated in the split form), then a pairwise
+//    tree across the CTA.
 //
 // Both are templated on the form:
 //  * MODE 0 (FP64): FP64 storage and FMA.
@@ -32,6 +36,13 @@ __device__ __forceinline__ int64_t deposit(const int64_t* s, uint64_t x) {
     off += s[i];
     x &= x - 1;
   }
+  return off;
+}
+
+__device__ __forceinline__ int64_t dep(const Runs& r, uint64_t x) {
+  int64_t off = 0;
+  for (int i = 0; i < r.n; ++i)
+    off += (int64_t)((x >> r.src[i]) & ((1ull << r.len[i]) - 1)) << r.dst[i];
   return off;
 }
 
@@ -85,26 +96,39 @@ __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ Joi
       mn = (uint64_t)idx & mnmask;
       const uint64_t m = mn >> jd.nb, n = mn & nmask;
       const int64_t s = s0 + b;
-      const T* pa = A + slice_offset(jd.a, b, s) + deposit(jd.a.s_outer, m);
-      const T* pb = B + slice_offset(jd.b, b, s) + deposit(jd.b.s_outer, n);
-      T fa = 1, fb = 1;
+      const int64_t oa = slice_offset(jd.a, b, s) + dep(jd.a.r_outer, m);
+      const int64_t ob = slice_offset(jd.b, b, s) + dep(jd.b.r_outer, n);
+      const T* pa = A + oa;
+      const T* pb = B + ob;
+      int64_t ka = 0, kb = 0;
       if (MODE == 1) {
         sa = op_shift(jd.a, b);
         sb = op_shift(jd.b, b);
-        fa = (T)pow2f(sa);
-        fb = (T)pow2f(sb);
-      }
-      int64_t ka = 0, kb = 0;
-      for (int k = 0; k < K; ++k) {
-        if (MODE == 1)
-          acc = fmaf((float)pa[ka] * (float)fa, (float)pb[kb] * (float)fb, (float)acc);
-        else
+        const float fa = pow2f(sa), fb = pow2f(sb);
+        // Leaf operands carry an FP32 residual: a*(hi+lo) = a*hi + a*lo keeps
+        // the leaf weights' rounding from becoming a per-variable bias.
+        const float* alo = jd.a.ptr_lo ? (const float*)jd.a.ptr_lo + oa : nullptr;
+        const float* blo = jd.b.ptr_lo ? (const float*)jd.b.ptr_lo + ob : nullptr;
+        float f = 0.f;
+        for (int k = 0; k < K; ++k) {
+          const float av = (float)pa[ka] * fa, bv = (float)pb[kb] * fb;
+          if (alo) f = fmaf(alo[ka] * fa, bv, f);
+          if (blo) f = fmaf(av, blo[kb] * fb, f);
+          f = fmaf(av, bv, f);
+          const int t = __ffs(~k) - 1;
+          ka += jd.a.dk[t];
+          kb += jd.b.dk[t];
+        }
+        acc = (T)f;
+      } else {
+        for (int k = 0; k < K; ++k) {
           acc = fma(pa[ka], pb[kb], acc);
-        const int t = __ffs(~k) - 1;
-        ka += jd.a.dk[t];
-        kb += jd.b.dk[t];
+          const int t = __ffs(~k) - 1;
+          ka += jd.a.dk[t];
+          kb += jd.b.dk[t];
+        }
       }
-      C[(int64_t)b * jd.c_batch_stride + deposit(jd.c_s_m, m) + deposit(jd.c_s_n, n)] = acc;
+      C[(int64_t)b * jd.c_batch_stride + dep(jd.r_cm, m) + dep(jd.r_cn, n)] = acc;
     }
     if (MODE == 1) {
       uint32_t bits = valid ? __float_as_uint((float)acc) : 0u;
@@ -113,6 +137,15 @@ __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ Joi
       if (valid && mn == 0) jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - sa - sb;
     }
   }
+}
+
+__device__ __forceinline__ void load4(const float* p, float* v) {
+  const float4 x = *reinterpret_cast<const float4*>(p);
+  v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+}
+__device__ __forceinline__ void load4(const double* p, double* v) {
+  const double2 x = reinterpret_cast<const double2*>(p)[0], y = reinterpret_cast<const double2*>(p)[1];
+  v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
 }
 
 template <int MODE, class T>
@@ -196,10 +229,8 @@ __global__ void __launch_bounds__(kThreads) k_tiled(const __grid_constant__ Join
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
       T av[4], bv[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) av[i] = As[kk][ty * 4 + i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx * 4 + j];
+      load4(&As[kk][ty * 4], av);
+      load4(&Bs[kk][tx * 4], bv);
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -236,6 +267,84 @@ __global__ void __launch_bounds__(kThreads) k_tiled(const __grid_constant__ Join
   }
 }
 
+// One CTA per (slice, output entry): thread t sums k = t, t+256, ... (k bits
+// below 8 come from t, the rest advance with the dk deltas), then a pairwise
+// tree over the CTA.  The split form keeps a Kahan-compensated FP32 partial.
+template <int MODE, class T>
+__global__ void __launch_bounds__(kThreads) k_reduce(const __grid_constant__ JoinDesc jd,
+                                                     const int64_t* __restrict__ d_s0, int nslices) {
+  constexpr int LOGT = 8;  // kThreads == 1 << LOGT
+  __shared__ double red_hi[kThreads / 32];
+  __shared__ double red_lo[kThreads / 32];
+  const int mnb = jd.mb + jd.nb;
+  const int64_t blk = blockIdx.x + (int64_t)blockIdx.y * gridDim.x;
+  const int b = (int)(blk >> mnb);
+  if (b >= nslices) return;
+  const uint64_t mn = (uint64_t)blk & ((1ull << mnb) - 1);
+  const uint64_t m = mn >> jd.nb, n = mn & ((1ull << jd.nb) - 1);
+  const int64_t s = (d_s0 ? *d_s0 : 0) + b;
+  const int tid = threadIdx.x;
+  const int64_t oa = slice_offset(jd.a, b, s) + dep(jd.a.r_outer, m);
+  const int64_t ob = slice_offset(jd.b, b, s) + dep(jd.b.r_outer, n);
+  const T* __restrict__ A = (const T*)jd.a.ptr + oa;
+  const T* __restrict__ B = (const T*)jd.b.ptr + ob;
+  // Offsets of k = tid, and the per-step delta when k advances by 2^LOGT.
+  int64_t ka = dep(jd.a.r_k, (uint64_t)tid), kb = dep(jd.b.r_k, (uint64_t)tid);
+  int64_t pa8 = 0, pb8 = 0;
+  for (int i = 0; i < LOGT && i < jd.kb; ++i) { pa8 += jd.a.s_k[i]; pb8 += jd.b.s_k[i]; }
+  const int64_t steps = (jd.kb > LOGT) ? (1ll << (jd.kb - LOGT)) : (tid < (1 << jd.kb) ? 1 : 0);
+  int sa = 0, sb = 0;
+  double hi = 0.0, lo = 0.0;
+  if (MODE == 1) {
+    sa = op_shift(jd.a, b);
+    sb = op_shift(jd.b, b);
+    const float fa = pow2f(sa), fb = pow2f(sb);
+    const float* alo = jd.a.ptr_lo ? (const float*)jd.a.ptr_lo + oa : nullptr;
+    const float* blo = jd.b.ptr_lo ? (const float*)jd.b.ptr_lo + ob : nullptr;
+    float sum = 0.f, c = 0.f;
+    for (int64_t j = 0; j < steps; ++j) {
+      const float av = (float)A[ka] * fa, bv = (float)B[kb] * fb;
+      float y = av * bv;
+      if (alo) y = fmaf(alo[ka] * fa, bv, y);
+      if (blo) y = fmaf(av, blo[kb] * fb, y);
+      y -= c;
+      const float t = sum + y;
+      c = (t - sum) - y;
+      sum = t;
+      const int t8 = __ffsll(~(unsigned long long)j) - 1 + LOGT;
+      if (t8 < TOGB_MAXBITS) { ka += jd.a.dk[t8] + pa8; kb += jd.b.dk[t8] + pb8; }
+    }
+    hi = (double)sum;
+    lo = -(double)c;
+  } else {
+    double sum = 0.0;
+    for (int64_t j = 0; j < steps; ++j) {
+      sum = fma((double)A[ka], (double)B[kb], sum);
+      const int t8 = __ffsll(~(unsigned long long)j) - 1 + LOGT;
+      if (t8 < TOGB_MAXBITS) { ka += jd.a.dk[t8] + pa8; kb += jd.b.dk[t8] + pb8; }
+    }
+    hi = sum;
+  }
+  // Pairwise tree: warp shuffles, then across warps.
+  for (int off = 16; off > 0; off >>= 1) {
+    hi += __shfl_xor_sync(0xffffffffu, hi, off);
+    lo += __shfl_xor_sync(0xffffffffu, lo, off);
+  }
+  if ((tid & 31) == 0) { red_hi[tid >> 5] = hi; red_lo[tid >> 5] = lo; }
+  __syncthreads();
+  if (tid == 0) {
+    double h = 0.0, l = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) { h += red_hi[w]; l += red_lo[w]; }
+    const double total = h + l;
+    T* C = (T*)jd.c_ptr + (int64_t)b * jd.c_batch_stride + dep(jd.r_cm, m) + dep(jd.r_cn, n);
+    *C = (T)total;
+    if (MODE == 1) {
+      atomicMax(&jd.c_max[b], __float_as_uint((float)total));
+      if (mn == 0) jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - sa - sb;
+    }
+  }
+}
+
 // Compensated (Neumaier) accumulation of every slice's root tensor, in slice
 // order, into the FP64 accumulator.
 template <int MODE, class T>
@@ -245,10 +354,14 @@ __global__ void k_root(const __grid_constant__ RootDesc rd, const int64_t* __res
   const T* __restrict__ R = (const T*)rd.r.ptr;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
     double sum = rd.acc_sum[e], comp = rd.acc_comp[e];
-    const int64_t oe = deposit(rd.r.s_outer, (uint64_t)e);
+    const int64_t oe = dep(rd.r.r_outer, (uint64_t)e);
     for (int b = 0; b < nslices; ++b) {
-      double x = (double)R[slice_offset(rd.r, b, s0 + b) + oe];
-      if (MODE == 1) x = ldexp(x, op_exp(rd.r, b));
+      const int64_t o = slice_offset(rd.r, b, s0 + b) + oe;
+      double x = (double)R[o];
+      if (MODE == 1) {
+        if (rd.r.ptr_lo) x += (double)((const float*)rd.r.ptr_lo)[o];
+        x = ldexp(x, op_exp(rd.r, b));
+      }
       const double t = sum + x;
       if (fabs(sum) >= fabs(x)) comp += (sum - t) + x; else comp += (x - t) + sum;
       sum = t;
@@ -293,6 +406,13 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
     dim3 grid((unsigned)tiles, gy, gz);
     if (mode == 0) k_tiled<0, double><<<grid, kThreads, 0, st>>>(jd, s0, nslices, tn_bits);
     else k_tiled<1, float><<<grid, kThreads, 0, st>>>(jd, s0, nslices, tn_bits);
+  } else if (kernel == K_REDUCE) {
+    const int64_t blocks = (int64_t)nslices << (jd.mb + jd.nb);
+    const unsigned gx = (unsigned)(blocks < 65536 ? blocks : 65536);
+    const unsigned gy = (unsigned)((blocks + gx - 1) / gx);
+    if (gy > 65535) return cudaErrorInvalidValue;
+    if (mode == 0) k_reduce<0, double><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
+    else k_reduce<1, float><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
   } else {
     const int64_t work = (int64_t)nslices << (jd.mb + jd.nb);
     const int g = grid_for(work);

@@ -65,7 +65,37 @@ struct Node {
 
 int64_t pow2(int r) { return int64_t(1) << r; }
 
+int log2_exact(int64_t v) {
+  int l = 0;
+  while ((int64_t(1) << l) < v) ++l;
+  return l;
+}
+
+// Kernel for a join in a given form.  Long-K joins with few outputs get the
+// CTA-per-output reduction; GEMM-sized joins the tiled kernel; the rest the
+// thread-per-output kernel.
+int choose_kernel(int mb, int nb, int kb) {
+  if (kb >= 12 && mb + nb <= 6) return togb::K_REDUCE;
+  if (mb >= 6 && nb >= 6 && kb >= 4) return togb::K_TILED;
+  return togb::K_DIRECT;
+}
+
 }  // namespace
+
+void togb::make_runs(const int64_t* s, int nbits, Runs* out) {
+  std::memset(out, 0, sizeof(*out));
+  int i = 0;
+  while (i < nbits) {
+    const int d = log2_exact(s[i]);
+    int len = 1;
+    while (i + len < nbits && s[i + len] == (s[i] << len)) ++len;
+    out->src[out->n] = (int8_t)i;
+    out->len[out->n] = (int8_t)len;
+    out->dst[out->n] = (int8_t)d;
+    ++out->n;
+    i += len;
+  }
+}
 
 struct togb_program {
   int device = 0;
@@ -81,7 +111,8 @@ struct togb_program {
   std::vector<int64_t> leaf_off;
   std::vector<int> leaf_shift;  // split mode normaliser per leaf
   double* d_leaf64 = nullptr;
-  float* d_leaf32 = nullptr;
+  float* d_leaf32 = nullptr;    // split mode: FP32 rounding of each leaf value
+  float* d_leaf32lo = nullptr;  // split mode: value - hi, rounded to FP32
   // planning
   int64_t arena = 0;  // per-slice elements
   double flops = 0, bytes64 = 0;
@@ -152,7 +183,7 @@ void plan_join(togb_program* p, Node& J) {
   for (int i = 0; i < nb; ++i) J.stride[J.n_lsb[i]] = pow2(i);
   for (size_t i = 0; i < J.m_lsb.size(); ++i) J.stride[J.m_lsb[i]] = pow2(nb + (int)i);
   const int mb = (int)J.m_lsb.size(), kb = (int)J.k_lsb.size();
-  J.kernel = (mb >= 6 && nb >= 6 && kb >= 4) ? togb::K_TILED : togb::K_DIRECT;
+  J.kernel = choose_kernel(mb, nb, kb);
   const double M = std::ldexp(1.0, mb), N = std::ldexp(1.0, nb), K = std::ldexp(1.0, kb);
   p->flops += 2.0 * M * N * K;
   p->bytes64 += 8.0 * (M * K + K * N + M * N);
@@ -207,6 +238,7 @@ void fill_operand(const togb_program* p, const Node& X, const std::vector<int>& 
     }
     od.n_slice_terms = nt;
     od.leaf_shift = p->leaf_shift[X.leaf];
+    if (mode == TOGB_MODE_SPLIT) od.ptr_lo = p->d_leaf32lo + p->leaf_off[X.leaf];
   } else {
     od.ptr = ws + X.off * (int64_t)B * es;
     od.batch_stride = pow2(X.rank);
@@ -231,6 +263,8 @@ void fill_operand(const togb_program* p, const Node& X, const std::vector<int>& 
     prefix += od.s_k[i];
   }
   od.k_fast = min_k < min_outer ? 1 : 0;
+  togb::make_runs(od.s_outer, od.outer_bits, &od.r_outer);
+  togb::make_runs(od.s_k, od.k_bits, &od.r_k);
 }
 
 void build_descs(togb_program* p, int mode, void* ws_v, int B) {
@@ -251,6 +285,8 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
     jd.c_batch_stride = pow2(J.rank);
     for (int i = 0; i < jd.mb; ++i) jd.c_s_m[i] = J.stride.at(J.m_lsb[i]);
     for (int i = 0; i < jd.nb; ++i) jd.c_s_n[i] = J.stride.at(J.n_lsb[i]);
+    togb::make_runs(jd.c_s_m, jd.mb, &jd.r_cm);
+    togb::make_runs(jd.c_s_n, jd.nb, &jd.r_cn);
     if (mode == TOGB_MODE_SPLIT) {
       char* meta = ws + p->arena * (int64_t)B * es;
       jd.c_exp = (int32_t*)meta + (int64_t)j * B;
@@ -279,7 +315,13 @@ togb_status enqueue_chunk(togb_program* p, int mode, int nb, cudaStream_t st,
   for (size_t j = 0; j < p->joins.size(); ++j) {
     if (ev) TOGB_CUDA(cudaEventRecord((*ev)[j], st));
     const Node& J = p->nodes[p->joins[j]];
-    cudaError_t e = togb::launch_join(mode, J.kernel, p->jds[j], p->d_s0, nb, st);
+    int kernel = J.kernel;
+    // The tiled kernel stages one value per element; leaf operands in the
+    // split form need their residual, which the other two kernels apply.
+    if (mode == TOGB_MODE_SPLIT && kernel == togb::K_TILED &&
+        (p->nodes[J.left].leaf >= 0 || p->nodes[J.right].leaf >= 0))
+      kernel = togb::K_DIRECT;
+    cudaError_t e = togb::launch_join(mode, kernel, p->jds[j], p->d_s0, nb, st);
     if (e != cudaSuccess) return cuda_fail(e, "join kernel launch");
   }
   if (ev) TOGB_CUDA(cudaEventRecord((*ev)[p->joins.size()], st));
@@ -388,15 +430,20 @@ togb_status togb_program_create(const togb_program_desc* d, int device, togb_pro
   // Device side.
   cudaError_t e = cudaSetDevice(device);
   if (e != cudaSuccess) { delete p; return cuda_fail(e, "cudaSetDevice"); }
-  std::vector<float> v32(voff);
-  for (int64_t i = 0; i < voff; ++i) v32[i] = (float)d->leaf_values[i];
+  std::vector<float> v32(voff), v32lo(voff);
+  for (int64_t i = 0; i < voff; ++i) {
+    v32[i] = (float)d->leaf_values[i];
+    v32lo[i] = (float)(d->leaf_values[i] - (double)v32[i]);
+  }
   const int64_t E = pow2(p->nodes[p->root].rank);
   if ((e = cudaMalloc(&p->d_leaf64, std::max<int64_t>(voff, 1) * 8)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_leaf32, std::max<int64_t>(voff, 1) * 4)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_leaf32lo, std::max<int64_t>(voff, 1) * 4)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_acc, 2 * E * 8)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_s0, 8)) != cudaSuccess ||
       (e = cudaMemcpy(p->d_leaf64, d->leaf_values, voff * 8, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(p->d_leaf32, v32.data(), voff * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(p->d_leaf32lo, v32lo.data(), voff * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemset(p->d_acc, 0, 2 * E * 8)) != cudaSuccess ||
       (e = cudaMemset(p->d_s0, 0, 8)) != cudaSuccess ||
       (e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking)) != cudaSuccess) {
@@ -547,6 +594,7 @@ void togb_program_destroy(togb_program* p) {
   clear_graphs(p);
   cudaFree(p->d_leaf64);
   cudaFree(p->d_leaf32);
+  cudaFree(p->d_leaf32lo);
   cudaFree(p->d_acc);
   cudaFree(p->d_s0);
   if (p->own_ws) cudaFree(p->own_ws);
@@ -593,6 +641,10 @@ togb_status togb_tensordot_f64(const double* a, int32_t ra, const double* b, int
   for (int i = 0; i < jd.nb; ++i) mino_b = std::min(mino_b, jd.b.s_outer[i]);
   jd.a.k_fast = mina < mino_a;
   jd.b.k_fast = minb < mino_b;
+  togb::make_runs(jd.a.s_outer, jd.mb, &jd.a.r_outer);
+  togb::make_runs(jd.a.s_k, jd.kb, &jd.a.r_k);
+  togb::make_runs(jd.b.s_outer, jd.nb, &jd.b.r_outer);
+  togb::make_runs(jd.b.s_k, jd.kb, &jd.b.r_k);
   jd.a.ptr = a;
   jd.b.ptr = b;
   jd.a.outer_bits = jd.mb; jd.a.k_bits = jd.kb;
@@ -603,7 +655,9 @@ togb_status togb_tensordot_f64(const double* a, int32_t ra, const double* b, int
   jd.c_batch_stride = pow2(jd.mb + jd.nb);
   for (int i = 0; i < jd.nb; ++i) jd.c_s_n[i] = pow2(i);
   for (int i = 0; i < jd.mb; ++i) jd.c_s_m[i] = pow2(jd.nb + i);
-  const int kernel = (jd.mb >= 6 && jd.nb >= 6 && jd.kb >= 4) ? togb::K_TILED : togb::K_DIRECT;
+  togb::make_runs(jd.c_s_m, jd.mb, &jd.r_cm);
+  togb::make_runs(jd.c_s_n, jd.nb, &jd.r_cn);
+  const int kernel = choose_kernel(jd.mb, jd.nb, jd.kb);
   cudaError_t e = togb::launch_join(TOGB_MODE_F64, kernel, jd, nullptr, 1, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "tensordot launch");
   return TOGB_OK;
