@@ -1,0 +1,42 @@
+"""The plugin inside the reference's own CLI (tensororder.py run): registration
+makes --tensor_library gb300 / gb300-split resolve, and the Execution stage
+hands the plugin the planned network.  Needs the reference checkout and the
+oracle build (python oracle/build_ref.py); skipped elsewhere.  The device call
+is replaced by the oracle here -- this test checks the wiring, not the compute
+(the GPU parity tests check the compute)."""
+import io
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from oracle import refload
+
+pytestmark = pytest.mark.skipif(not refload.available(), reason="reference checkout / oracle build absent")
+
+
+@pytest.mark.parametrize("library,mode", [("gb300", 0), ("gb300-split", 1)])
+def test_cli_selects_plugin(library, mode, monkeypatch, capsys):
+    refload.load()
+    from oracle import contract
+    from tensororder_gb300 import api, launcher
+
+    calls = []
+
+    def stub(self, prog, limit):
+        calls.append((prog.num_joins, prog.num_slices, self._mode))
+        return np.asarray(contract.contract_sliced(prog, limit))
+
+    monkeypatch.setattr(api.GB300API, "_run", stub)
+    cnf = os.path.join(refload.reference_src(), "..", "benchmarks", "cubic_vertex_cover", "cubic_vc_50_0.cnf")
+    monkeypatch.setattr(sys, "stdin", io.StringIO(open(cnf).read()))
+    monkeypatch.chdir(refload.REF_OUT)
+    with pytest.raises(SystemExit) as exc:
+        launcher.main(["--reference-src", refload.reference_src(), "tensororder", "--planner", "line-Flow",
+                       "--weights", "unweighted", "--tensor_library", library, "--timeout", "3",
+                       "--minimum_slice", "2"])
+    assert exc.value.code == 0
+    out = capsys.readouterr().out
+    assert "Count: 2802717837" in out
+    assert len(calls) == 1 and calls[0][1] == 4 and calls[0][2] == mode
