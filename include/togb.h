@@ -121,6 +121,26 @@ togb_status togb_tensordot_f64(const double* a, int32_t rank_a, const double* b,
  * achieved FLOP/s measured with CUDA events on `stream`. */
 togb_status togb_probe_peak(int kind, void* stream, double* flops_per_second);
 
+/* Size of the device scratch array behind togb_contract_static_f64. */
+#define TOGB_STATIC_SCRATCH_BYTES (32u << 20)
+
+/* Contract a whole program in FP64 without allocating device memory.  This
+ * entry point has no counterpart in the reference.  It serves callers that
+ * cannot call cudaMalloc -- processes whose device memory all belongs to their
+ * own allocator, or pipelines that cannot afford the device synchronisation
+ * cudaMalloc/cudaFree imply.  The caller passes the program (host arrays;
+ * desc->leaf_values may be NULL), the leaf values already on the current
+ * device (same concatenated layout as desc->leaf_values), and `d_out`, device
+ * memory for the 2^root_rank compensated sums over all slices.  Intermediates
+ * live in one file-scope device array of TOGB_STATIC_SCRATCH_BYTES (32 MiB),
+ * held by every GPU that loads the library until exit; a program that needs
+ * more than that for a single slice is rejected with TOGB_ERR_OOM and a message
+ * giving both sizes.  The first call on a device looks up the array's address
+ * (make it before any stream capture).  All calls share the array: calls whose
+ * work overlaps on the GPU race, so serialise them.  Queued on `stream`. */
+togb_status togb_contract_static_f64(const togb_program_desc* desc, const double* d_leaf_values,
+                                     double* d_out, void* stream);
+
 const char* togb_last_error(void);
 int togb_version(void);
 

@@ -85,6 +85,20 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
                         cudaStream_t st);
 cudaError_t launch_root(int mode, const RootDesc& rd, const int64_t* s0, int nslices, cudaStream_t st);
 cudaError_t launch_set_s0(int64_t* d_s0, int64_t value, cudaStream_t st);
+// out[e] = acc[e] + acc[E + e]: the compensated sum of a root accumulator.
+cudaError_t launch_finalize(const double* acc, int64_t E, double* out, cudaStream_t st);
 cudaError_t probe_peak(int kind, cudaStream_t st, double* flops);
+
+}  // namespace togb
+
+#include "togb.h"
+
+namespace togb {
+
+// FP64 contraction of a whole program inside `scratch` (togb_runtime.cpp).
+togb_status static_contract_f64(const togb_program_desc* d, const double* d_leaf, char* scratch,
+                                size_t scratch_bytes, double* d_out, cudaStream_t st);
+// Record `msg` as the calling thread's last error and return `st`.
+togb_status report(togb_status st, const char* msg);
 
 }  // namespace togb

@@ -373,6 +373,11 @@ __global__ void k_root(const __grid_constant__ RootDesc rd, const int64_t* __res
 
 __global__ void k_set_s0(int64_t* p, int64_t v) { *p = v; }
 
+__global__ void k_finalize(const double* __restrict__ acc, int64_t E, double* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = acc[e] + acc[E + e];
+}
+
 template <class T>
 __global__ void __launch_bounds__(kThreads) k_probe(T* out, int iters, T seed) {
   T a0 = seed + (T)threadIdx.x, a1 = a0 + (T)1, a2 = a0 + (T)2, a3 = a0 + (T)3;
@@ -431,6 +436,11 @@ cudaError_t launch_root(int mode, const RootDesc& rd, const int64_t* s0, int nsl
 
 cudaError_t launch_set_s0(int64_t* d_s0, int64_t value, cudaStream_t st) {
   k_set_s0<<<1, 1, 0, st>>>(d_s0, value);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const double* acc, int64_t E, double* out, cudaStream_t st) {
+  k_finalize<<<grid_for(E), kThreads, 0, st>>>(acc, E, out);
   return cudaGetLastError();
 }
 

@@ -338,7 +338,13 @@ int togb_version(void) { return 1; }
 
 const char* togb_last_error(void) { return g_err.c_str(); }
 
-togb_status togb_program_create(const togb_program_desc* d, int device, togb_program** out) {
+}  // extern "C"
+
+namespace {
+
+// Host half of togb_program_create: validation, lowering and planning.  No
+// device memory is touched.  Leaf values are validated only when present.
+togb_status lower_host(const togb_program_desc* d, int device, togb_program** out, int64_t* num_values) {
   if (!d || !out) return fail(TOGB_ERR_INVALID, "null argument");
   *out = nullptr;
   if (d->num_leaves <= 0 || d->num_tokens <= 0) return fail(TOGB_ERR_INVALID, "empty program");
@@ -372,7 +378,7 @@ togb_status togb_program_create(const togb_program_desc* d, int device, togb_pro
     ax += r;
     p->leaf_off[l] = voff;
     double mx = 0;
-    for (int64_t i = 0; i < pow2(r); ++i) {
+    for (int64_t i = 0; d->leaf_values && i < pow2(r); ++i) {
       const double v = d->leaf_values[voff + i];
       if (!(v >= 0) || std::isinf(v)) {
         delete p;
@@ -426,6 +432,23 @@ togb_status togb_program_create(const togb_program_desc* d, int device, togb_pro
   p->root = stack[0];
   for (const Node& n : p->nodes) p->max_rank = std::max(p->max_rank, n.rank);
   plan_arena(p);
+  *num_values = voff;
+  *out = p;
+  return TOGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+togb_status togb_program_create(const togb_program_desc* d, int device, togb_program** out) {
+  if (!d || !out) return fail(TOGB_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (!d->leaf_values) return fail(TOGB_ERR_INVALID, "null leaf values");
+  togb_program* p = nullptr;
+  int64_t voff = 0;
+  togb_status st = lower_host(d, device, &p, &voff);
+  if (st != TOGB_OK) return st;
 
   // Device side.
   cudaError_t e = cudaSetDevice(device);
@@ -671,3 +694,47 @@ togb_status togb_probe_peak(int kind, void* stream, double* flops) {
 }
 
 }  // extern "C"
+
+// Contraction of a whole program in FP64 with every intermediate inside a
+// caller-supplied scratch region (the library's static device array).  Layout:
+// [slice base, 256 B][accumulator: 2 * 2^root_rank doubles, rounded up to
+// 256 B][arena: per-slice arena * chunk].  No device memory is allocated.
+togb_status togb::static_contract_f64(const togb_program_desc* d, const double* d_leaf, char* scratch,
+                                      size_t scratch_bytes, double* d_out, cudaStream_t st) {
+  togb_program* p = nullptr;
+  int64_t nvals = 0;
+  togb_status r = lower_host(d, 0, &p, &nvals);
+  if (r != TOGB_OK) return r;
+  const int64_t E = pow2(p->nodes[p->root].rank);
+  const int64_t head = 256 + (2 * E * 8 + 255) / 256 * 256;
+  const int64_t per = p->arena * 8;
+  if (head + per > (int64_t)scratch_bytes) {
+    const std::string msg = "program needs " + std::to_string(head + per) +
+                            " bytes of device scratch for one slice; the static scratch holds " +
+                            std::to_string(scratch_bytes) + " bytes";
+    delete p;
+    return fail(TOGB_ERR_OOM, msg);
+  }
+  const int64_t B = std::min<int64_t>({((int64_t)scratch_bytes - head) / per, p->num_slices, 65535});
+  p->d_leaf64 = const_cast<double*>(d_leaf);
+  p->d_s0 = (int64_t*)scratch;
+  p->d_acc = (double*)(scratch + 256);
+  build_descs(p, TOGB_MODE_F64, scratch + head, (int)B);
+  p->cur_B = (int)B;
+  togb_status out = TOGB_OK;
+  cudaError_t e = cudaMemsetAsync(p->d_acc, 0, 2 * E * 8, st);
+  if (e != cudaSuccess) out = cuda_fail(e, "accumulator clear");
+  for (int64_t s = 0; out == TOGB_OK && s < p->num_slices; s += B) {
+    const int nb = (int)std::min<int64_t>(B, p->num_slices - s);
+    e = togb::launch_set_s0(p->d_s0, s, st);
+    if (e != cudaSuccess) { out = cuda_fail(e, "slice base update"); break; }
+    out = enqueue_chunk(p, TOGB_MODE_F64, nb, st, nullptr);
+  }
+  if (out == TOGB_OK && (e = togb::launch_finalize(p->d_acc, E, d_out, st)) != cudaSuccess)
+    out = cuda_fail(e, "result write");
+  // Every device pointer above is borrowed; the host object owns none.
+  delete p;
+  return out;
+}
+
+togb_status togb::report(togb_status st, const char* msg) { return fail(st, msg); }

@@ -69,7 +69,10 @@ EXPORTS = [
     "togb_version", "togb_last_error", "togb_program_create", "togb_program_info_get",
     "togb_program_reset", "togb_program_run", "togb_program_result", "togb_program_set_timing",
     "togb_program_join_times", "togb_program_destroy", "togb_tensordot_f64", "togb_probe_peak",
+    "togb_contract_static_f64",
 ]
+
+STATIC_SCRATCH_BYTES = 32 << 20
 
 
 def library_path():
@@ -100,6 +103,7 @@ def lib():
     L.togb_tensordot_f64.argtypes = [c_void, ctypes.c_int32, c_void, ctypes.c_int32, ctypes.c_int32,
                                      _i32p, _i32p, c_void, c_void]
     L.togb_probe_peak.argtypes = [ctypes.c_int, c_void, ctypes.POINTER(ctypes.c_double)]
+    L.togb_contract_static_f64.argtypes = [ctypes.POINTER(ProgramDesc), c_void, c_void, c_void]
     for name in EXPORTS:
         if name not in ("togb_version", "togb_last_error", "togb_program_destroy"):
             getattr(L, name).restype = ctypes.c_int
@@ -249,3 +253,24 @@ def probe_peak(kind, stream=None):
     v = ctypes.c_double()
     check(lib().togb_probe_peak(int(kind), _stream_handle(stream), ctypes.byref(v)))
     return v.value
+
+
+def contract_static_f64(program: Program, leaf_values, out, stream=None):
+    """FP64 contraction through ``togb_contract_static_f64``: no device memory
+    is allocated by the library.  ``leaf_values`` is a float64 CUDA tensor with
+    the concatenated leaf parents (``DeviceProgram``'s layout) and ``out`` a
+    float64 CUDA tensor of ``2**root_rank`` entries; both belong to the caller.
+    Calls that overlap on the GPU share one scratch array and must not run
+    concurrently."""
+    leaves = program.leaves
+    ranks = np.array([l.rank for l in leaves], dtype=np.int32)
+    axes = np.array([a for l in leaves for a in l.axes] or [0], dtype=np.int32)
+    tokens = np.array(program.postorder, dtype=np.int32)
+    gsize = np.array([len(g) for g in program.slice_groups] or [0], dtype=np.int32)
+    gedges = np.array([e for g in program.slice_groups for e in g] or [0], dtype=np.int32)
+    desc = ProgramDesc(len(leaves), ranks.ctypes.data_as(_i32p), axes.ctypes.data_as(_i32p), None,
+                       len(tokens), tokens.ctypes.data_as(_i32p), len(program.slice_groups),
+                       gsize.ctypes.data_as(_i32p), gedges.ctypes.data_as(_i32p))
+    check(lib().togb_contract_static_f64(ctypes.byref(desc), ctypes.c_void_p(leaf_values.data_ptr()),
+                                         ctypes.c_void_p(out.data_ptr()), _stream_handle(stream)))
+    return out

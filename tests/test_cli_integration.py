@@ -29,6 +29,7 @@ def test_cli_selects_plugin(library, mode, monkeypatch, capsys):
         return np.asarray(contract.contract_sliced(prog, limit))
 
     monkeypatch.setattr(api.GB300API, "_run", stub)
+    monkeypatch.setattr(api, "_OOM", api._OOM)  # register() rebinds it; restore afterwards
     cnf = os.path.join(refload.reference_src(), "..", "benchmarks", "cubic_vertex_cover", "cubic_vc_50_0.cnf")
     monkeypatch.setattr(sys, "stdin", io.StringIO(open(cnf).read()))
     monkeypatch.chdir(refload.REF_OUT)

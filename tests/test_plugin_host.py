@@ -81,5 +81,5 @@ def test_oom_maps_to_reference_error(monkeypatch):
     monkeypatch.setitem(sys.modules, "torch", types.SimpleNamespace(cuda=types.SimpleNamespace(
         current_stream=lambda *a: None)))
     prog = Program.from_dict(load_golden("wvc18_s2")["program"])
-    with pytest.raises(api.OutOfMemoryError):
+    with pytest.raises(api._OOM):
         api.GB300API().contract_program(prog)
