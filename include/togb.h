@@ -116,9 +116,10 @@ togb_status togb_tensordot_f64(const double* a, int32_t rank_a, const double* b,
                                int32_t n_axes, const int32_t* axes_a, const int32_t* axes_b,
                                double* out, void* stream);
 
-/* Device throughput probe used for roofline denominators: runs a dependent
- * FMA chain kernel of `kind` (0 = FP64 FFMA, 1 = FP32 FFMA) and returns the
- * achieved FLOP/s measured with CUDA events on `stream`. */
+/* Device throughput probe used for roofline denominators: runs independent
+ * FMA chains of `kind` (0 = FP64 FMA, 1 = FP32 FMA, 2 = FP64 mma.sync m8n8k4)
+ * on every SM and returns the achieved FLOP/s measured with CUDA events on
+ * `stream`. */
 togb_status togb_probe_peak(int kind, void* stream, double* flops_per_second);
 
 /* Size of the device scratch array behind togb_contract_static_f64. */

@@ -16,6 +16,7 @@
 // of the global slice index is set (SlicedTensor.build, tensor.py:66-68).
 #pragma once
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #define TOGB_MAXBITS 32
@@ -49,6 +50,7 @@ struct OpDesc {
   const void* ptr_lo;        // split mode, leaves: FP32 residual (value - hi), same layout
   Runs r_outer;              // run form of s_outer
   Runs r_k;                  // run form of s_k
+  int32_t ktab[16];          // dep_k(k) for k < min(K, 16)
 };
 
 struct JoinDesc {
@@ -62,6 +64,9 @@ struct JoinDesc {
   int32_t* c_exp;      // split mode: per-slice exponent of the output
   uint32_t* c_max;     // split mode: per-slice max bits of the output (zeroed before the join)
   Runs r_cm, r_cn;     // run forms of c_s_m / c_s_n
+  int32_t c_natural;   // output stored C[m][n] row-major, slices contiguous: address = linear index
+  Runs r_inv_m, r_inv_n;  // output address bits -> m / n bits (inverse deposit of c_s_m / c_s_n)
+  int32_t* err;        // device error word: set to 1 when a bounded wait gives up (may be null)
 };
 
 // Root reduction: adds every slice's root tensor into the compensated FP64
@@ -74,16 +79,24 @@ struct RootDesc {
 
 namespace togb {
 
-enum Kernel { K_DIRECT = 0, K_TILED = 1, K_REDUCE = 2 };
+enum Kernel { K_DIRECT = 0, K_TILED = 1, K_REDUCE = 2, K_UMMA = 3 };
 
 // Host helper: run form of a stride table (strides must be powers of two).
 void make_runs(const int64_t* s, int nbits, Runs* out);
+// Host helper: runs mapping the output address bits owned by one GEMM index
+// (strides s[0..nbits)) back to that index's bits.
+void make_inverse_runs(const int64_t* s, int nbits, Runs* out);
 
 // Launchers (togb_kernels.cu).  `s0` points at the global index of the first
 // slice of the chunk; `nslices` is the number of slices in the chunk.
 cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t* s0, int nslices,
                         cudaStream_t st);
 cudaError_t launch_root(int mode, const RootDesc& rd, const int64_t* s0, int nslices, cudaStream_t st);
+// Split-form GEMM on the tensor cores (togb_umma.cu): 3xTF32, TMEM accumulators.
+// `ta`/`tb` are TMA maps of plain K-major operands (k, row, slice), or null to
+// gather through the deposit layouts.
+cudaError_t launch_umma(const JoinDesc& jd, const CUtensorMap* ta, const CUtensorMap* tb, const int64_t* s0,
+                        int nslices, cudaStream_t st);
 cudaError_t launch_set_s0(int64_t* d_s0, int64_t value, cudaStream_t st);
 // out[e] = acc[e] + acc[E + e]: the compensated sum of a root accumulator.
 cudaError_t launch_finalize(const double* acc, int64_t E, double* out, cudaStream_t st);

@@ -23,59 +23,97 @@
 #include <cuda_runtime.h>
 
 #include "togb_internal.h"
+#include "togb_device.cuh"
 
 namespace togb {
 namespace {
 
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ int64_t deposit(const int64_t* s, uint64_t x) {
-  int64_t off = 0;
-  while (x) {
-    const int i = __ffsll((long long)x) - 1;
-    off += s[i];
-    x &= x - 1;
+// Dot product of one output over K.  KK > 0: K == KK <= 16, offsets from the
+// per-join table and every load issued before the FMAs; KK == 0: any K, offsets
+// advanced with the dk deltas.  Split form: inputs scaled by fa/fb (exact powers
+// of two), leaf residuals folded in.
+template <int MODE, class T, int KK>
+__device__ __forceinline__ T dot_k(const JoinDesc& jd, const T* __restrict__ A, const T* __restrict__ B,
+                                   int64_t oa, int64_t ob, int K, float fa, float fb) {
+  if constexpr (KK > 0) {
+    T av[KK], bv[KK];
+#pragma unroll
+    for (int k = 0; k < KK; ++k) {
+      av[k] = A[oa + jd.a.ktab[k]];
+      bv[k] = B[ob + jd.b.ktab[k]];
+    }
+    if (MODE == 1) {
+      float f = 0.f;
+      if (jd.a.ptr_lo) {
+        const float* lo = (const float*)jd.a.ptr_lo + oa;
+#pragma unroll
+        for (int k = 0; k < KK; ++k) f = fmaf(lo[jd.a.ktab[k]] * fa, (float)bv[k] * fb, f);
+      }
+      if (jd.b.ptr_lo) {
+        const float* lo = (const float*)jd.b.ptr_lo + ob;
+#pragma unroll
+        for (int k = 0; k < KK; ++k) f = fmaf((float)av[k] * fa, lo[jd.b.ktab[k]] * fb, f);
+      }
+#pragma unroll
+      for (int k = 0; k < KK; ++k) f = fmaf((float)av[k] * fa, (float)bv[k] * fb, f);
+      return (T)f;
+    } else {
+      T acc = 0;
+#pragma unroll
+      for (int k = 0; k < KK; ++k) acc = fma(av[k], bv[k], acc);
+      return acc;
+    }
+  } else {
+    int64_t ka = 0, kb = 0;
+    if (MODE == 1) {
+      const float* alo = jd.a.ptr_lo ? (const float*)jd.a.ptr_lo + oa : nullptr;
+      const float* blo = jd.b.ptr_lo ? (const float*)jd.b.ptr_lo + ob : nullptr;
+      float f = 0.f;
+      for (int k = 0; k < K; ++k) {
+        const float av = (float)A[oa + ka] * fa, bv = (float)B[ob + kb] * fb;
+        if (alo) f = fmaf(alo[ka] * fa, bv, f);
+        if (blo) f = fmaf(av, blo[kb] * fb, f);
+        f = fmaf(av, bv, f);
+        const int t = __ffs(~k) - 1;
+        ka += jd.a.dk[t];
+        kb += jd.b.dk[t];
+      }
+      return (T)f;
+    } else {
+      T acc = 0;
+      for (int k = 0; k < K; ++k) {
+        acc = fma(A[oa + ka], B[ob + kb], acc);
+        const int t = __ffs(~k) - 1;
+        ka += jd.a.dk[t];
+        kb += jd.b.dk[t];
+      }
+      return acc;
+    }
   }
-  return off;
 }
 
-__device__ __forceinline__ int64_t dep(const Runs& r, uint64_t x) {
-  int64_t off = 0;
-  for (int i = 0; i < r.n; ++i)
-    off += (int64_t)((x >> r.src[i]) & ((1ull << r.len[i]) - 1)) << r.dst[i];
-  return off;
+__device__ __forceinline__ void store_vec(float* p, const float* v) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void store_vec(double* p, const double* v) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
 }
 
-__device__ __forceinline__ int64_t slice_offset(const OpDesc& o, int b, int64_t s) {
-  if (o.batch_stride) return (int64_t)b * o.batch_stride;
-  int64_t off = 0;
-  for (int j = 0; j < o.n_slice_terms; ++j)
-    if ((s >> o.slice_shift[j]) & 1) off += o.slice_stride[j];
-  return off;
-}
-
-// Power-of-two normaliser that brings a slice maximum into [1, 2).
-__device__ __forceinline__ int shift_from_max(uint32_t bits) {
-  if (bits == 0) return 0;
-  const int e = (int)((bits >> 23) & 0xff);
-  int sh = (e == 0) ? 126 : 127 - e;
-  return max(-126, min(126, sh));
-}
-
-__device__ __forceinline__ float pow2f(int sh) { return __int_as_float((127 + sh) << 23); }
-
-__device__ __forceinline__ int op_shift(const OpDesc& o, int b) {
-  return o.max_ptr ? shift_from_max(o.max_ptr[b]) : o.leaf_shift;
-}
-
-__device__ __forceinline__ int op_exp(const OpDesc& o, int b) { return o.exp_ptr ? o.exp_ptr[b] : 0; }
-
-template <int MODE, class T>
+// Thread-per-output kernel: each thread computes VEC consecutive outputs in
+// the output's own address order (slice-major), recovering (m, n) from the
+// address with the inverse runs, so every store is a contiguous vector store
+// whatever order the consumer asked for; 2*VEC*K loads are in flight at once.
+template <int MODE, class T, int KK, int VEC>
 __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ JoinDesc jd,
                                                      const int64_t* __restrict__ d_s0, int nslices) {
   const int mnb = jd.mb + jd.nb;
-  const int64_t total = (int64_t)nslices << mnb;
-  const int64_t total_pad = (total + 31) & ~(int64_t)31;
+  const int64_t groups = ((int64_t)nslices << mnb) / VEC;
+  const int64_t groups_pad = (groups + 31) & ~(int64_t)31;
+  const int64_t per_slice = (1ll << mnb) / VEC;  // groups per slice (power of two)
+  const int lanes = per_slice >= 32 ? 32 : (int)per_slice;
   const int64_t s0 = d_s0 ? *d_s0 : 0;
   const int K = 1 << jd.kb;
   const T* __restrict__ A = (const T*)jd.a.ptr;
@@ -83,58 +121,48 @@ __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ Joi
   T* __restrict__ C = (T*)jd.c_ptr;
   const uint64_t nmask = (1ull << jd.nb) - 1;
   const uint64_t mnmask = (1ull << mnb) - 1;
-  const int group = mnb >= 5 ? 32 : (1 << mnb);  // lanes that share one slice
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total_pad;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const bool valid = idx < total;
-    T acc = 0;
-    int b = 0;
-    uint64_t mn = 0;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < groups_pad;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const bool valid = g < groups;
+    const int64_t idx0 = g * VEC;
+    const int b = valid ? (int)(idx0 >> mnb) : 0;
+    uint32_t bits = 0;
     int sa = 0, sb = 0;
     if (valid) {
-      b = (int)(idx >> mnb);
-      mn = (uint64_t)idx & mnmask;
-      const uint64_t m = mn >> jd.nb, n = mn & nmask;
       const int64_t s = s0 + b;
-      const int64_t oa = slice_offset(jd.a, b, s) + dep(jd.a.r_outer, m);
-      const int64_t ob = slice_offset(jd.b, b, s) + dep(jd.b.r_outer, n);
-      const T* pa = A + oa;
-      const T* pb = B + ob;
-      int64_t ka = 0, kb = 0;
+      const int64_t soa = slice_offset(jd.a, b, s), sob = slice_offset(jd.b, b, s);
+      float fa = 1.f, fb = 1.f;
       if (MODE == 1) {
         sa = op_shift(jd.a, b);
         sb = op_shift(jd.b, b);
-        const float fa = pow2f(sa), fb = pow2f(sb);
-        // Leaf operands carry an FP32 residual: a*(hi+lo) = a*hi + a*lo keeps
-        // the leaf weights' rounding from becoming a per-variable bias.
-        const float* alo = jd.a.ptr_lo ? (const float*)jd.a.ptr_lo + oa : nullptr;
-        const float* blo = jd.b.ptr_lo ? (const float*)jd.b.ptr_lo + ob : nullptr;
-        float f = 0.f;
-        for (int k = 0; k < K; ++k) {
-          const float av = (float)pa[ka] * fa, bv = (float)pb[kb] * fb;
-          if (alo) f = fmaf(alo[ka] * fa, bv, f);
-          if (blo) f = fmaf(av, blo[kb] * fb, f);
-          f = fmaf(av, bv, f);
-          const int t = __ffs(~k) - 1;
-          ka += jd.a.dk[t];
-          kb += jd.b.dk[t];
-        }
-        acc = (T)f;
-      } else {
-        for (int k = 0; k < K; ++k) {
-          acc = fma(pa[ka], pb[kb], acc);
-          const int t = __ffs(~k) - 1;
-          ka += jd.a.dk[t];
-          kb += jd.b.dk[t];
-        }
+        fa = pow2f(sa);
+        fb = pow2f(sb);
       }
-      C[(int64_t)b * jd.c_batch_stride + dep(jd.r_cm, m) + dep(jd.r_cn, n)] = acc;
+      T out[VEC];
+#pragma unroll
+      for (int j = 0; j < VEC; ++j) {
+        const uint64_t q = (uint64_t)(idx0 + j) & mnmask;  // output address within the slice
+        const uint64_t m = jd.c_natural ? (q >> jd.nb) : (uint64_t)dep(jd.r_inv_m, q);
+        const uint64_t n = jd.c_natural ? (q & nmask) : (uint64_t)dep(jd.r_inv_n, q);
+        const int64_t oa = soa + dep(jd.a.r_outer, m);
+        const int64_t ob = sob + dep(jd.b.r_outer, n);
+        out[j] = dot_k<MODE, T, KK>(jd, A, B, oa, ob, K, fa, fb);
+      }
+      if (VEC == 4) {
+        store_vec(C + idx0, out);  // program outputs are dense per slice: address = linear index
+      } else {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) C[idx0 + j] = out[j];
+      }
+      if (MODE == 1) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) bits = max(bits, __float_as_uint((float)out[j]));
+        if ((idx0 & (int64_t)mnmask) == 0) jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - sa - sb;
+      }
     }
     if (MODE == 1) {
-      uint32_t bits = valid ? __float_as_uint((float)acc) : 0u;
-      for (int off = 1; off < group; off <<= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, off));
-      if (valid && (threadIdx.x & (group - 1)) == 0) atomicMax(&jd.c_max[b], bits);
-      if (valid && mn == 0) jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - sa - sb;
+      for (int off = 1; off < lanes; off <<= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, off));
+      if (valid && (threadIdx.x & (lanes - 1)) == 0) atomicMax(&jd.c_max[b], bits);
     }
   }
 }
@@ -302,26 +330,50 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const __grid_constant__ Joi
     const float* alo = jd.a.ptr_lo ? (const float*)jd.a.ptr_lo + oa : nullptr;
     const float* blo = jd.b.ptr_lo ? (const float*)jd.b.ptr_lo + ob : nullptr;
     float sum = 0.f, c = 0.f;
-    for (int64_t j = 0; j < steps; ++j) {
-      const float av = (float)A[ka] * fa, bv = (float)B[kb] * fb;
-      float y = av * bv;
-      if (alo) y = fmaf(alo[ka] * fa, bv, y);
-      if (blo) y = fmaf(av, blo[kb] * fb, y);
-      y -= c;
-      const float t = sum + y;
-      c = (t - sum) - y;
-      sum = t;
-      const int t8 = __ffsll(~(unsigned long long)j) - 1 + LOGT;
-      if (t8 < TOGB_MAXBITS) { ka += jd.a.dk[t8] + pa8; kb += jd.b.dk[t8] + pb8; }
+    constexpr int U = 4;
+    for (int64_t j0 = 0; j0 < steps; j0 += U) {
+      int64_t oa_[U], ob_[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        oa_[u] = ka;
+        ob_[u] = kb;
+        const int t8 = __ffsll(~(unsigned long long)(j0 + u)) - 1 + LOGT;
+        if (t8 < TOGB_MAXBITS) { ka += jd.a.dk[t8] + pa8; kb += jd.b.dk[t8] + pb8; }
+      }
+      float y[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        y[u] = 0.f;
+        if (j0 + u < steps) {
+          const float av = (float)A[oa_[u]] * fa, bv = (float)B[ob_[u]] * fb;
+          y[u] = av * bv;
+          if (alo) y[u] = fmaf(alo[oa_[u]] * fa, bv, y[u]);
+          if (blo) y[u] = fmaf(av, blo[ob_[u]] * fb, y[u]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const float yy = y[u] - c;
+        const float t = sum + yy;
+        c = (t - sum) - yy;
+        sum = t;
+      }
     }
     hi = (double)sum;
     lo = -(double)c;
   } else {
     double sum = 0.0;
-    for (int64_t j = 0; j < steps; ++j) {
-      sum = fma((double)A[ka], (double)B[kb], sum);
-      const int t8 = __ffsll(~(unsigned long long)j) - 1 + LOGT;
-      if (t8 < TOGB_MAXBITS) { ka += jd.a.dk[t8] + pa8; kb += jd.b.dk[t8] + pb8; }
+    constexpr int U = 4;
+    for (int64_t j0 = 0; j0 < steps; j0 += U) {
+      double y[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        y[u] = (j0 + u < steps) ? (double)A[ka] * (double)B[kb] : 0.0;
+        const int t8 = __ffsll(~(unsigned long long)(j0 + u)) - 1 + LOGT;
+        if (t8 < TOGB_MAXBITS) { ka += jd.a.dk[t8] + pa8; kb += jd.b.dk[t8] + pb8; }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) sum += y[u];
     }
     hi = sum;
   }
@@ -380,15 +432,39 @@ __global__ void k_finalize(const double* __restrict__ acc, int64_t E, double* __
 
 template <class T>
 __global__ void __launch_bounds__(kThreads) k_probe(T* out, int iters, T seed) {
-  T a0 = seed + (T)threadIdx.x, a1 = a0 + (T)1, a2 = a0 + (T)2, a3 = a0 + (T)3;
-  T a4 = a0 + (T)4, a5 = a0 + (T)5, a6 = a0 + (T)6, a7 = a0 + (T)7;
+  T a[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) a[i] = seed + (T)(threadIdx.x + i);
   const T m = (T)0.999999, c = (T)1e-7;
   for (int i = 0; i < iters; ++i) {
-    a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
-    a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int j = 0; j < 16; ++j) a[j] = fma(a[j], m, c);
   }
-  const T r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  T r = 0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) r += a[i];
   if (r == (T)-1) out[0] = r;
+}
+
+// FP64 tensor-core probe: independent mma.sync m8n8k4 FP64 accumulations.
+__global__ void __launch_bounds__(kThreads) k_probe_dmma(double* out, int iters) {
+  double a = 1.0 + threadIdx.x * 1e-6, b = 0.5;
+  double c[8][2];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) { c[i][0] = 0.0; c[i][1] = 0.0; }
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+                   : "+d"(c[i][0]), "+d"(c[i][1])
+                   : "d"(a), "d"(b));
+  }
+  double r = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r += c[i][0] + c[i][1];
+  if (r == -1.0) out[0] = r;
 }
 
 int grid_for(int64_t work) {
@@ -401,7 +477,8 @@ int grid_for(int64_t work) {
 
 cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t* s0, int nslices,
                         cudaStream_t st) {
-  if (kernel == K_TILED) {
+  if (kernel == K_UMMA && mode == 1) return launch_umma(jd, nullptr, nullptr, s0, nslices, st);
+  if (kernel == K_TILED || kernel == K_UMMA) {
     const int tm_bits = jd.mb > 6 ? jd.mb - 6 : 0;
     const int tn_bits = jd.nb > 6 ? jd.nb - 6 : 0;
     const uint64_t tiles = 1ull << (tm_bits + tn_bits);
@@ -419,10 +496,27 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
     if (mode == 0) k_reduce<0, double><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
     else k_reduce<1, float><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
   } else {
-    const int64_t work = (int64_t)nslices << (jd.mb + jd.nb);
-    const int g = grid_for(work);
-    if (mode == 0) k_direct<0, double><<<g, kThreads, 0, st>>>(jd, s0, nslices);
-    else k_direct<1, float><<<g, kThreads, 0, st>>>(jd, s0, nslices);
+    const int mnb = jd.mb + jd.nb;
+    const int vec = mnb >= 2 ? 4 : 1;
+    const int64_t groups = ((int64_t)nslices << mnb) / vec;
+    const int g = grid_for(groups);
+#define TOGB_DIRECT(KK)                                                                          \
+    if (vec == 4) {                                                                              \
+      if (mode == 0) k_direct<0, double, KK, 4><<<g, kThreads, 0, st>>>(jd, s0, nslices);       \
+      else k_direct<1, float, KK, 4><<<g, kThreads, 0, st>>>(jd, s0, nslices);                  \
+    } else {                                                                                     \
+      if (mode == 0) k_direct<0, double, KK, 1><<<g, kThreads, 0, st>>>(jd, s0, nslices);       \
+      else k_direct<1, float, KK, 1><<<g, kThreads, 0, st>>>(jd, s0, nslices);                  \
+    }
+    switch (jd.kb) {
+      case 0: TOGB_DIRECT(1) break;
+      case 1: TOGB_DIRECT(2) break;
+      case 2: TOGB_DIRECT(4) break;
+      case 3: TOGB_DIRECT(8) break;
+      case 4: TOGB_DIRECT(16) break;
+      default: TOGB_DIRECT(0) break;
+    }
+#undef TOGB_DIRECT
   }
   return cudaGetLastError();
 }
@@ -452,14 +546,15 @@ cudaError_t probe_peak(int kind, cudaStream_t st, double* flops) {
   cudaError_t e = cudaMalloc(&out, 16);
   if (e != cudaSuccess) return e;
   const int blocks = sms * 8;
-  const int iters = kind == 0 ? 4096 : 65536;
+  const int iters = kind == 0 ? 512 : (kind == 1 ? 16384 : 2048);
   cudaEvent_t t0, t1;
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
-  for (int rep = 0; rep < 2; ++rep) {  // first pass warms clocks
+  for (int rep = 0; rep < 2; ++rep) {  // the first pass brings the clocks up
     cudaEventRecord(t0, st);
     if (kind == 0) k_probe<double><<<blocks, kThreads, 0, st>>>((double*)out, iters, 1.0);
-    else k_probe<float><<<blocks, kThreads, 0, st>>>((float*)out, iters, 1.0f);
+    else if (kind == 1) k_probe<float><<<blocks, kThreads, 0, st>>>((float*)out, iters, 1.0f);
+    else k_probe_dmma<<<blocks, kThreads, 0, st>>>((double*)out, iters);
     cudaEventRecord(t1, st);
   }
   e = cudaEventSynchronize(t1);
@@ -469,7 +564,10 @@ cudaError_t probe_peak(int kind, cudaStream_t st, double* flops) {
   cudaEventDestroy(t1);
   cudaFree(out);
   if (e != cudaSuccess) return e;
-  *flops = 2.0 * 8.0 * iters * (double)blocks * kThreads / (ms * 1e-3);
+  const double threads = (double)blocks * kThreads;
+  const double work = kind == 2 ? threads / 32.0 * 8.0 * iters * 512.0   // FLOP per warp-mma: 2*8*8*4
+                                : threads * 2.0 * 64.0 * iters;
+  *flops = work / (ms * 1e-3);
   return cudaGetLastError();
 }
 

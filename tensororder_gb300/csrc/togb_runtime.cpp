@@ -15,6 +15,7 @@
 //  * the FP64 slice sum of BaseTensorAPI.contract_sliced
 //    (src/tensor_network/tensor_apis/base_api.py:21-28), done here with a
 //    compensated sum on the device.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -97,6 +98,26 @@ void togb::make_runs(const int64_t* s, int nbits, Runs* out) {
   }
 }
 
+void togb::make_inverse_runs(const int64_t* s, int nbits, Runs* out) {
+  // (address bit, index bit) pairs sorted by address bit, then merged into runs.
+  std::vector<std::pair<int, int>> bits;
+  for (int i = 0; i < nbits; ++i) bits.push_back({log2_exact(s[i]), i});
+  std::sort(bits.begin(), bits.end());
+  std::memset(out, 0, sizeof(*out));
+  size_t i = 0;
+  while (i < bits.size()) {
+    int len = 1;
+    while (i + len < bits.size() && bits[i + len].first == bits[i].first + len &&
+           bits[i + len].second == bits[i].second + len)
+      ++len;
+    out->src[out->n] = (int8_t)bits[i].first;
+    out->len[out->n] = (int8_t)len;
+    out->dst[out->n] = (int8_t)bits[i].second;
+    ++out->n;
+    i += len;
+  }
+}
+
 struct togb_program {
   int device = 0;
   int G = 0;
@@ -120,6 +141,7 @@ struct togb_program {
   // device state
   double* d_acc = nullptr;  // [2 * 2^root_rank]: sum then compensation
   int64_t* d_s0 = nullptr;
+  int32_t* d_err = nullptr; // set by a kernel whose bounded wait expired
   void* own_ws = nullptr;
   size_t own_ws_bytes = 0;
   cudaStream_t cap_stream = nullptr;
@@ -128,6 +150,8 @@ struct togb_program {
   int cur_B = 0;
   const void* cur_ws = nullptr;
   std::vector<JoinDesc> jds;
+  std::vector<CUtensorMap> tmaps;  // per join: TMA maps of A and B (tensor-core joins with plain operands)
+  std::vector<char> use_tma;
   RootDesc rd{};
   uint32_t* d_max = nullptr;  // split mode max bits [joins][B] inside the workspace
   size_t max_bytes = 0;
@@ -154,7 +178,10 @@ void clear_graphs(togb_program* p) {
   p->graphs.clear();
 }
 
-// Choose the GEMM bit orders of a join and its output layout.
+// Bottom-up part of a join's plan: edge sets, reference output order, kernel,
+// cost, and a natural layout -- GEMM bit orders following the operands'
+// strides (monotone reads) and the output stored C[m][n].  plan_layouts may
+// later replace the layout of joins that feed a GEMM-shaped consumer.
 void plan_join(togb_program* p, Node& J) {
   const Node& L = p->nodes[J.left];
   const Node& R = p->nodes[J.right];
@@ -178,7 +205,6 @@ void plan_join(togb_program* p, Node& J) {
   J.k_lsb = shared;
   const Node& big = (L.rank >= R.rank) ? L : R;
   std::sort(J.k_lsb.begin(), J.k_lsb.end(), by_stride(big));
-  // Output stored as C[m][n] row-major: n bits lowest.
   const int nb = (int)J.n_lsb.size();
   for (int i = 0; i < nb; ++i) J.stride[J.n_lsb[i]] = pow2(i);
   for (size_t i = 0; i < J.m_lsb.size(); ++i) J.stride[J.m_lsb[i]] = pow2(nb + (int)i);
@@ -187,6 +213,58 @@ void plan_join(togb_program* p, Node& J) {
   const double M = std::ldexp(1.0, mb), N = std::ldexp(1.0, nb), K = std::ldexp(1.0, kb);
   p->flops += 2.0 * M * N * K;
   p->bytes64 += 8.0 * (M * K + K * N + M * N);
+}
+
+// Top-down layout requests.  A GEMM-shaped join (tiled / tensor-core kernels)
+// or a long-K reduction asks for its intermediate operands in [free][shared]
+// order with one shared-axis order on both sides, so it reads two row-major
+// K-major matrices; the producers then write their outputs in that order (a
+// producer's free axes keep their significance from the requested order, so
+// its stores follow its loads).  Every other join keeps the natural layout of
+// plan_join, which favours the thread-per-output kernel's reads.  A leaf
+// operand's layout is its parent tensor's, so it fixes the shared-axis order.
+void plan_layouts(togb_program* p) {
+  std::vector<std::vector<int>> req(p->nodes.size());  // requested order, most significant first
+  std::vector<char> requested(p->nodes.size(), 0);
+  auto in = [](const std::vector<int>& v, int e) { return std::find(v.begin(), v.end(), e) != v.end(); };
+  for (auto it = p->joins.rbegin(); it != p->joins.rend(); ++it) {
+    Node& J = p->nodes[*it];
+    std::vector<int> mu, nu;  // most significant first
+    if (requested[*it]) {
+      const std::vector<int>& sigma = req[*it];
+      const int r = (int)sigma.size();
+      for (int q = 0; q < r; ++q) J.stride[sigma[q]] = pow2(r - 1 - q);
+      for (int e : sigma) {
+        if (in(J.m_lsb, e)) mu.push_back(e);
+        else nu.push_back(e);
+      }
+    } else {
+      mu.assign(J.m_lsb.rbegin(), J.m_lsb.rend());
+      nu.assign(J.n_lsb.rbegin(), J.n_lsb.rend());
+    }
+    J.m_lsb.assign(mu.rbegin(), mu.rend());
+    J.n_lsb.assign(nu.rbegin(), nu.rend());
+    if (J.kernel != togb::K_TILED && J.kernel != togb::K_REDUCE) continue;
+    const Node& L = p->nodes[J.left];
+    const Node& R = p->nodes[J.right];
+    std::vector<int> kappa = J.k_lsb;
+    const Node* leaf = L.leaf >= 0 ? &L : (R.leaf >= 0 ? &R : nullptr);
+    if (leaf)
+      std::sort(kappa.begin(), kappa.end(), [leaf](int a, int b) { return leaf->stride.at(a) > leaf->stride.at(b); });
+    else
+      std::sort(kappa.begin(), kappa.end());
+    if (L.leaf < 0) {
+      req[J.left] = mu;
+      req[J.left].insert(req[J.left].end(), kappa.begin(), kappa.end());
+      requested[J.left] = 1;
+    }
+    if (R.leaf < 0) {
+      req[J.right] = nu;
+      req[J.right].insert(req[J.right].end(), kappa.begin(), kappa.end());
+      requested[J.right] = 1;
+    }
+    J.k_lsb.assign(kappa.rbegin(), kappa.rend());
+  }
 }
 
 // First-fit arena over the join outputs, freeing operands after their consumer.
@@ -216,6 +294,25 @@ void plan_arena(togb_program* p) {
       if (p->nodes[opnd].leaf < 0) release(p->nodes[opnd].off);
   }
   p->arena = std::max<int64_t>(top, kAlignElems);
+}
+
+// dep_k(k) for the first 16 values of k (the unrolled small-K kernels).
+void fill_ktab(OpDesc& od) {
+  for (int k = 0; k < 16; ++k) {
+    int64_t off = 0;
+    for (int i = 0; i < od.k_bits; ++i)
+      if ((k >> i) & 1) off += od.s_k[i];
+    od.ktab[k] = (k < (1 << std::min(od.k_bits, 4))) ? (int32_t)off : 0;
+  }
+}
+
+// True when C is stored [slice][m][n] row-major, i.e. address = linear index.
+int is_natural(const JoinDesc& jd) {
+  for (int i = 0; i < jd.nb; ++i)
+    if (jd.c_s_n[i] != pow2(i)) return 0;
+  for (int i = 0; i < jd.mb; ++i)
+    if (jd.c_s_m[i] != pow2(jd.nb + i)) return 0;
+  return jd.c_batch_stride == pow2(jd.mb + jd.nb) ? 1 : 0;
 }
 
 void fill_operand(const togb_program* p, const Node& X, const std::vector<int>& outer,
@@ -265,12 +362,79 @@ void fill_operand(const togb_program* p, const Node& X, const std::vector<int>& 
   od.k_fast = min_k < min_outer ? 1 : 0;
   togb::make_runs(od.s_outer, od.outer_bits, &od.r_outer);
   togb::make_runs(od.s_k, od.k_bits, &od.r_k);
+  fill_ktab(od);
+}
+
+// Kernel for a join in the split form: GEMM-sized joins of two intermediates
+// go to the tensor cores; leaf operands need their FP32 residual, which only
+// the CUDA-core kernels apply.
+int split_kernel(const togb_program* p, const Node& J) {
+  const bool leaf = p->nodes[J.left].leaf >= 0 || p->nodes[J.right].leaf >= 0;
+  if (J.kernel == togb::K_TILED) return leaf ? togb::K_DIRECT : togb::K_UMMA;
+  return J.kernel;
+}
+
+// An intermediate operand stored as a row-major [rows][K] matrix per slice.
+bool plain_k_major(const OpDesc& o) {
+  if (o.batch_stride == 0) return false;  // leaf: read from its parent tensor
+  for (int i = 0; i < o.k_bits; ++i)
+    if (o.s_k[i] != pow2(i)) return false;
+  for (int i = 0; i < o.outer_bits; ++i)
+    if (o.s_outer[i] != pow2(o.k_bits + i)) return false;
+  return o.batch_stride == pow2(o.k_bits + o.outer_bits);
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)f;
+    cudaGetLastError();
+  }
+  return fn;
+}
+
+// TMA map of a plain FP32 operand: dims (k, row, slice), box (32, box_rows, 1),
+// 128-byte swizzle (the K-major SWIZZLE_128B operand layout of tcgen05.mma).
+bool make_tmap(const OpDesc& o, int nslices, uint32_t box_rows, CUtensorMap* out) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return false;
+  const cuuint64_t K = (cuuint64_t)pow2(o.k_bits), R = (cuuint64_t)pow2(o.outer_bits);
+  const cuuint64_t dims[3] = {K, R, (cuuint64_t)nslices};
+  const cuuint64_t strides[2] = {K * 4, K * R * 4};
+  const cuuint32_t box[3] = {32, box_rows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  if ((K * 4) % 16 != 0 || ((uintptr_t)o.ptr % 16) != 0) return false;
+  return fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(o.ptr), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// C = A.B^T computed as (B.A^T)^T: exchange the operands and the output's m/n strides.
+void swap_operands(JoinDesc& jd) {
+  std::swap(jd.a, jd.b);
+  std::swap(jd.mb, jd.nb);
+  for (int i = 0; i < TOGB_MAXBITS; ++i) std::swap(jd.c_s_m[i], jd.c_s_n[i]);
+  std::swap(jd.r_cm, jd.r_cn);
+  std::swap(jd.r_inv_m, jd.r_inv_n);
+  jd.c_natural = 0;
 }
 
 void build_descs(togb_program* p, int mode, void* ws_v, int B) {
   char* ws = (char*)ws_v;
   const size_t es = elem_size(mode);
   p->jds.assign(p->joins.size(), JoinDesc{});
+  p->tmaps.assign(2 * p->joins.size(), CUtensorMap{});
+  p->use_tma.assign(p->joins.size(), 0);
   for (size_t j = 0; j < p->joins.size(); ++j) {
     const Node& J = p->nodes[p->joins[j]];
     JoinDesc& jd = p->jds[j];
@@ -287,10 +451,20 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
     for (int i = 0; i < jd.nb; ++i) jd.c_s_n[i] = J.stride.at(J.n_lsb[i]);
     togb::make_runs(jd.c_s_m, jd.mb, &jd.r_cm);
     togb::make_runs(jd.c_s_n, jd.nb, &jd.r_cn);
+    togb::make_inverse_runs(jd.c_s_m, jd.mb, &jd.r_inv_m);
+    togb::make_inverse_runs(jd.c_s_n, jd.nb, &jd.r_inv_n);
+    jd.c_natural = is_natural(jd);
+    jd.err = p->d_err;
     if (mode == TOGB_MODE_SPLIT) {
       char* meta = ws + p->arena * (int64_t)B * es;
       jd.c_exp = (int32_t*)meta + (int64_t)j * B;
       jd.c_max = (uint32_t*)(meta + 4 * (int64_t)p->joins.size() * B) + (int64_t)j * B;
+      // The tensor-core kernel tiles 128 rows of M: put the larger extent there.
+      if (split_kernel(p, J) == togb::K_UMMA) {
+        if (jd.mb < 7 && jd.nb > jd.mb) swap_operands(jd);
+        p->use_tma[j] = plain_k_major(jd.a) && plain_k_major(jd.b) && jd.kb >= 2 &&
+                        make_tmap(jd.a, B, 128, &p->tmaps[2 * j]) && make_tmap(jd.b, B, 64, &p->tmaps[2 * j + 1]);
+      }
     }
   }
   // Root: outer bits enumerate the reference axis order, last axis lowest.
@@ -315,13 +489,12 @@ togb_status enqueue_chunk(togb_program* p, int mode, int nb, cudaStream_t st,
   for (size_t j = 0; j < p->joins.size(); ++j) {
     if (ev) TOGB_CUDA(cudaEventRecord((*ev)[j], st));
     const Node& J = p->nodes[p->joins[j]];
-    int kernel = J.kernel;
-    // The tiled kernel stages one value per element; leaf operands in the
-    // split form need their residual, which the other two kernels apply.
-    if (mode == TOGB_MODE_SPLIT && kernel == togb::K_TILED &&
-        (p->nodes[J.left].leaf >= 0 || p->nodes[J.right].leaf >= 0))
-      kernel = togb::K_DIRECT;
-    cudaError_t e = togb::launch_join(mode, kernel, p->jds[j], p->d_s0, nb, st);
+    const int kernel = mode == TOGB_MODE_SPLIT ? split_kernel(p, J) : J.kernel;
+    cudaError_t e;
+    if (kernel == togb::K_UMMA && mode == TOGB_MODE_SPLIT && p->use_tma[j])
+      e = togb::launch_umma(p->jds[j], &p->tmaps[2 * j], &p->tmaps[2 * j + 1], p->d_s0, nb, st);
+    else
+      e = togb::launch_join(mode, kernel, p->jds[j], p->d_s0, nb, st);
     if (e != cudaSuccess) return cuda_fail(e, "join kernel launch");
   }
   if (ev) TOGB_CUDA(cudaEventRecord((*ev)[p->joins.size()], st));
@@ -431,6 +604,7 @@ togb_status lower_host(const togb_program_desc* d, int device, togb_program** ou
     if (!used[l]) { delete p; return fail(TOGB_ERR_INVALID, "leaf never pushed"); }
   p->root = stack[0];
   for (const Node& n : p->nodes) p->max_rank = std::max(p->max_rank, n.rank);
+  plan_layouts(p);
   plan_arena(p);
   *num_values = voff;
   *out = p;
@@ -464,6 +638,8 @@ togb_status togb_program_create(const togb_program_desc* d, int device, togb_pro
       (e = cudaMalloc(&p->d_leaf32lo, std::max<int64_t>(voff, 1) * 4)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_acc, 2 * E * 8)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_s0, 8)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_err, 4)) != cudaSuccess ||
+      (e = cudaMemset(p->d_err, 0, 4)) != cudaSuccess ||
       (e = cudaMemcpy(p->d_leaf64, d->leaf_values, voff * 8, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(p->d_leaf32, v32.data(), voff * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(p->d_leaf32lo, v32lo.data(), voff * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -602,6 +778,12 @@ togb_status togb_program_result(togb_program* p, void* stream, double* out, doub
   if (n != E) return fail(TOGB_ERR_INVALID, "result size does not match the root tensor");
   TOGB_CUDA(cudaSetDevice(p->device));
   TOGB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  int32_t err = 0;
+  TOGB_CUDA(cudaMemcpy(&err, p->d_err, 4, cudaMemcpyDeviceToHost));
+  if (err) {
+    TOGB_CUDA(cudaMemset(p->d_err, 0, 4));
+    return fail(TOGB_ERR_TIMEOUT, "a tensor-core kernel gave up waiting for its MMAs; the result is invalid");
+  }
   std::vector<double> h(2 * E);
   TOGB_CUDA(cudaMemcpy(h.data(), p->d_acc, 2 * E * 8, cudaMemcpyDeviceToHost));
   for (int64_t i = 0; i < E; ++i) {
@@ -620,6 +802,7 @@ void togb_program_destroy(togb_program* p) {
   cudaFree(p->d_leaf32lo);
   cudaFree(p->d_acc);
   cudaFree(p->d_s0);
+  cudaFree(p->d_err);
   if (p->own_ws) cudaFree(p->own_ws);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   delete p;
@@ -664,14 +847,16 @@ togb_status togb_tensordot_f64(const double* a, int32_t ra, const double* b, int
   for (int i = 0; i < jd.nb; ++i) mino_b = std::min(mino_b, jd.b.s_outer[i]);
   jd.a.k_fast = mina < mino_a;
   jd.b.k_fast = minb < mino_b;
+  jd.a.outer_bits = jd.mb; jd.a.k_bits = jd.kb;
+  jd.b.outer_bits = jd.nb; jd.b.k_bits = jd.kb;
   togb::make_runs(jd.a.s_outer, jd.mb, &jd.a.r_outer);
   togb::make_runs(jd.a.s_k, jd.kb, &jd.a.r_k);
   togb::make_runs(jd.b.s_outer, jd.nb, &jd.b.r_outer);
   togb::make_runs(jd.b.s_k, jd.kb, &jd.b.r_k);
+  fill_ktab(jd.a);
+  fill_ktab(jd.b);
   jd.a.ptr = a;
   jd.b.ptr = b;
-  jd.a.outer_bits = jd.mb; jd.a.k_bits = jd.kb;
-  jd.b.outer_bits = jd.nb; jd.b.k_bits = jd.kb;
   jd.a.batch_stride = pow2(ra);
   jd.b.batch_stride = pow2(rb);
   jd.c_ptr = out;
@@ -680,6 +865,9 @@ togb_status togb_tensordot_f64(const double* a, int32_t ra, const double* b, int
   for (int i = 0; i < jd.mb; ++i) jd.c_s_m[i] = pow2(jd.nb + i);
   togb::make_runs(jd.c_s_m, jd.mb, &jd.r_cm);
   togb::make_runs(jd.c_s_n, jd.nb, &jd.r_cn);
+  togb::make_inverse_runs(jd.c_s_m, jd.mb, &jd.r_inv_m);
+  togb::make_inverse_runs(jd.c_s_n, jd.nb, &jd.r_inv_n);
+  jd.c_natural = is_natural(jd);
   const int kernel = choose_kernel(jd.mb, jd.nb, jd.kb);
   cudaError_t e = togb::launch_join(TOGB_MODE_F64, kernel, jd, nullptr, 1, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "tensordot launch");
@@ -687,7 +875,7 @@ togb_status togb_tensordot_f64(const double* a, int32_t ra, const double* b, int
 }
 
 togb_status togb_probe_peak(int kind, void* stream, double* flops) {
-  if (!flops || (kind != 0 && kind != 1)) return fail(TOGB_ERR_INVALID, "bad probe arguments");
+  if (!flops || kind < 0 || kind > 2) return fail(TOGB_ERR_INVALID, "bad probe arguments");
   cudaError_t e = togb::probe_peak(kind, (cudaStream_t)stream, flops);
   if (e != cudaSuccess) return cuda_fail(e, "peak probe");
   return TOGB_OK;

@@ -1,0 +1,78 @@
+"""GEMM-shaped joins between two intermediates -- the joins the split form
+runs on the tensor cores (3xTF32, TMEM accumulators) and the plain form on the
+tiled FP64 kernel.  Seeded dense leaves in [0.5, 1.5] are joined pairwise into
+two intermediates X and Y, which are then contracted with M, N >= 64 and
+K >= 16 under random axis permutations; the full root tensor is compared with
+the numpy oracle.  Tolerances: 1e-12 (plain), 1e-6 (split), relative to the
+largest entry."""
+import numpy as np
+import pytest
+
+from oracle import contract as oracle
+from tensororder_gb300 import runtime
+from tensororder_gb300.program import Leaf, Program
+
+pytestmark = pytest.mark.gpu
+
+
+def make_program(seed, m, n, k, slices=0):
+    """X has axes (F_A | K), Y has axes (K | F_B), each built as the outer
+    product of two dense leaves; the root join contracts K."""
+    rng = np.random.default_rng(seed)
+    edges = list(range(m + n + k))
+    fa, fb, kk = edges[:m], edges[m:m + n], edges[m + n:]
+    x_axes = list(rng.permutation(fa + kk))
+    y_axes = list(rng.permutation(kk + fb))
+    # sliced edges: extra shared edges between the two halves of X (group g)
+    leaves = []
+
+    def halves(axes):
+        cut = len(axes) // 2
+        return axes[:cut], axes[cut:]
+
+    for axes in (x_axes, y_axes):
+        h1, h2 = halves(axes)
+        for h in (h1, h2):
+            leaves.append(Leaf(list(int(e) for e in h), "dense", values=rng.uniform(0.5, 1.5, size=(2,) * len(h))))
+    groups = []
+    if slices:
+        # slice edges joining the two halves of Y: add them to both Y leaves
+        base = len(edges)
+        for g in range(slices):
+            e = base + g
+            leaves[2].axes.append(e)
+            leaves[3].axes.append(e)
+            groups.append([e])
+        for l in leaves[2:]:
+            l.values = rng.uniform(0.5, 1.5, size=(2,) * l.rank)
+    prog = Program(leaves, [0, 1, -1, 2, 3, -1, -1], groups)
+    return prog.validate()
+
+
+SHAPES = [(6, 6, 4), (7, 7, 5), (8, 7, 6), (6, 8, 7), (9, 6, 4), (7, 9, 8), (8, 8, 9), (6, 6, 10)]
+
+
+@pytest.mark.parametrize("m,n,k", SHAPES)
+@pytest.mark.parametrize("mode,tol", [(runtime.MODE_F64, 1e-12), (runtime.MODE_SPLIT, 1e-6)])
+def test_gemm_join(m, n, k, mode, tol, cuda):
+    prog = make_program(1000 * m + 100 * n + k, m, n, k)
+    want = oracle.contract(prog, 0)[0]
+    dp = runtime.DeviceProgram(prog)
+    dp.reset()
+    dp.run(mode)
+    got = dp.result()
+    dp.close()
+    assert got.shape == want.shape
+    assert np.abs(got - want).max() <= tol * np.abs(want).max()
+
+
+@pytest.mark.parametrize("mode,tol", [(runtime.MODE_F64, 1e-12), (runtime.MODE_SPLIT, 1e-6)])
+def test_gemm_join_sliced(mode, tol, cuda):
+    prog = make_program(77, 7, 6, 5, slices=3)
+    want = sum(oracle.contract(prog, s)[0] for s in range(prog.num_slices))
+    dp = runtime.DeviceProgram(prog)
+    dp.reset()
+    dp.run(mode)
+    got = dp.result()
+    dp.close()
+    assert np.abs(got - want).max() <= tol * np.abs(want).max()
