@@ -243,18 +243,39 @@ def main():
         dp.set_timing(False)
         return t
 
-    from oracle import contract as oracle  # checker only: shapes of the joins
-
-    shapes = oracle.join_shapes(prog)
+    jinfo = dp.joins(runtime.MODE_SPLIT)  # (log2 M, log2 N, log2 K, kernel) per join
     jt_split = per_join(runtime.MODE_SPLIT, dp.allocate_workspace(runtime.MODE_SPLIT, S, 0.6))
     jt_plain = per_join(runtime.MODE_F64, dp.allocate_workspace(runtime.MODE_F64, S, 0.6))
     top = int(np.argmax(jt_split))
-    m, n, k = shapes[top]
+    mb, nb, kb, kern = (int(x) for x in jinfo[top])
+    m, n, k = 1 << mb, 1 << nb, 1 << kb
     top_flops = 2.0 * m * n * k * S
     top_bytes = 4.0 * (m * k + k * n + m * n) * S
     fp32_peak = runtime.probe_peak(1, stream)
     fp64_peak = runtime.probe_peak(0, stream)
+    tf32_peak = runtime.probe_peak(3, stream)
     peaks = measured_peaks()
+    by_kernel = {}
+    for j in range(len(jt_split)):
+        name = runtime.KERNEL_NAMES[int(jinfo[j][3])]
+        c, t = by_kernel.get(name, (0, 0.0))
+        by_kernel[name] = (c + 1, t + float(jt_split[j]))
+    if kern == 3:  # tensor cores: 3 TF32 MMAs per product
+        roof = {"bound": "tensor", "achieved": top_flops / (jt_split[top] * 1e-3) / 1e12,
+                "peak": tf32_peak / 3 / 1e12, "unit": "TFLOP/s",
+                "peak_source": "tcgen05 kind::tf32 probe measured in this run (%.0f TFLOP/s) / 3 MMAs per "
+                               "3xTF32 product" % (tf32_peak / 1e12),
+                "tensor_pipe_tflops": 3 * top_flops / (jt_split[top] * 1e-3) / 1e12,
+                "bf16_measured_tflops": peaks.get("bf16_tflops")}
+    else:  # memory-bound CUDA-core kernels
+        roof = {"bound": "hbm", "achieved": top_bytes / (jt_split[top] * 1e-3) / 1e9,
+                "peak": peaks.get("hbm_gbs") or 6800.0, "unit": "GB/s",
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks.get("hbm_gbs") else "fallback 6.8 TB/s"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof.update({"kernel": "join %d (M,N,K)=(%d,%d,%d) x %d slices, %s kernel, split form"
+                           % (top, m, n, k, S, runtime.KERNEL_NAMES[kern]),
+                 "share_of_step": float(jt_split[top] / jt_split.sum()),
+                 "traffic": None})
 
     # End to end through the plugin's public call: host program in, count out.
     backend = api.GB300SplitAPI(device=local)
@@ -294,19 +315,8 @@ def main():
         "plain_f64": {"ms_per_count": ms_plain, "counts_per_s": 1e3 / ms_plain,
                       "tflops": flops / (ms_plain * 1e-3) / 1e12, "rel_err": abs(plain_val - ref) / ref},
         "speedup_chosen_vs_plain": ms_plain / ms_split,
-        "roofline": {
-            "kernel": "join %d (M,N,K)=(%d,%d,%d) x %d slices, split form" % (top, m, n, k, S),
-            "bound": "fp32-fma",
-            "achieved": top_flops / (jt_split[top] * 1e-3) / 1e12,
-            "peak": fp32_peak / 1e12,
-            "unit": "TFLOP/s",
-            "frac": (top_flops / (jt_split[top] * 1e-3)) / fp32_peak,
-            "peak_source": "togb_probe_peak FP32 FMA chain, measured in this run",
-            "hbm_achieved_gbs": top_bytes / (jt_split[top] * 1e-3) / 1e9,
-            "hbm_peak_gbs": peaks.get("hbm_gbs"),
-            "share_of_step": float(jt_split[top] / jt_split.sum()),
-            "traffic": None,
-        },
+        "roofline": roof,
+        "step_by_kernel_ms": {kk: {"joins": c, "ms": round(t, 3)} for kk, (c, t) in by_kernel.items()},
         "fp64_roofline": {"achieved_tflops": flops / (ms_plain * 1e-3) / 1e12, "peak_tflops": fp64_peak / 1e12,
                           "frac": (flops / (ms_plain * 1e-3)) / fp64_peak,
                           "peak_source": "togb_probe_peak FP64 FMA chain, measured in this run"},
@@ -314,7 +324,7 @@ def main():
         "e2e": {"value": 1e3 / float(np.mean(e2e_ms)), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "path": "GB300SplitAPI.contract_program(host program) -> libtogb C ABI"},
-        "gpu_launches": int(info.num_launches) * args.steps,
+        "gpu_launches": (int(info.num_launches) + 1) * args.steps,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(prog)

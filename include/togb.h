@@ -101,6 +101,11 @@ togb_status togb_program_run(togb_program* prog, int mode, int64_t slice_begin, 
  * together with the compensation terms (`comp`, may be NULL). */
 togb_status togb_program_result(togb_program* prog, void* stream, double* out, double* comp, int64_t n);
 
+/* Per join in post-order, four int32: log2 M, log2 N, log2 K over unsliced
+ * axes and the kernel used in `mode` (0 thread-per-output, 1 tiled SIMT GEMM,
+ * 2 CTA-per-output reduction, 3 tensor-core GEMM).  n = num_joins. */
+togb_status togb_program_joins(const togb_program* prog, int mode, int32_t* out, int32_t n);
+
 /* Per-join device time of the last run with togb_program_set_timing(prog, 1):
  * `ms[j]` for each join in post-order (n = num_joins). */
 togb_status togb_program_set_timing(togb_program* prog, int enable);
@@ -116,10 +121,10 @@ togb_status togb_tensordot_f64(const double* a, int32_t rank_a, const double* b,
                                int32_t n_axes, const int32_t* axes_a, const int32_t* axes_b,
                                double* out, void* stream);
 
-/* Device throughput probe used for roofline denominators: runs independent
- * FMA chains of `kind` (0 = FP64 FMA, 1 = FP32 FMA, 2 = FP64 mma.sync m8n8k4)
- * on every SM and returns the achieved FLOP/s measured with CUDA events on
- * `stream`. */
+/* Device throughput probe used for roofline denominators: runs `kind` on
+ * every SM (0 = FP64 FMA chains, 1 = FP32 FMA chains, 2 = FP64 mma.sync
+ * m8n8k4, 3 = tcgen05.mma kind::tf32 128x256x8) and returns the achieved
+ * FLOP/s measured with CUDA events on `stream`. */
 togb_status togb_probe_peak(int kind, void* stream, double* flops_per_second);
 
 /* Size of the device scratch array behind togb_contract_static_f64. */

@@ -101,6 +101,8 @@ cudaError_t launch_set_s0(int64_t* d_s0, int64_t value, cudaStream_t st);
 // out[e] = acc[e] + acc[E + e]: the compensated sum of a root accumulator.
 cudaError_t launch_finalize(const double* acc, int64_t E, double* out, cudaStream_t st);
 cudaError_t probe_peak(int kind, cudaStream_t st, double* flops);
+// Tensor-pipe throughput of tcgen05 kind::tf32 MMAs (togb_umma.cu).
+cudaError_t probe_umma(cudaStream_t st, double* flops);
 
 }  // namespace togb
 

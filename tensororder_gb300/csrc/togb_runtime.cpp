@@ -677,6 +677,19 @@ togb_status togb_program_reset(togb_program* p, void* stream) {
   return TOGB_OK;
 }
 
+togb_status togb_program_joins(const togb_program* p, int mode, int32_t* out, int32_t n) {
+  if (!p || !out) return fail(TOGB_ERR_INVALID, "null argument");
+  if (n != (int32_t)p->joins.size()) return fail(TOGB_ERR_INVALID, "n must equal the number of joins");
+  for (size_t j = 0; j < p->joins.size(); ++j) {
+    const Node& J = p->nodes[p->joins[j]];
+    out[4 * j + 0] = (int32_t)J.m_lsb.size();
+    out[4 * j + 1] = (int32_t)J.n_lsb.size();
+    out[4 * j + 2] = (int32_t)J.k_lsb.size();
+    out[4 * j + 3] = mode == TOGB_MODE_SPLIT ? split_kernel(p, J) : J.kernel;
+  }
+  return TOGB_OK;
+}
+
 togb_status togb_program_set_timing(togb_program* p, int enable) {
   if (!p) return fail(TOGB_ERR_INVALID, "null program");
   p->timing = enable != 0;
@@ -875,8 +888,9 @@ togb_status togb_tensordot_f64(const double* a, int32_t ra, const double* b, int
 }
 
 togb_status togb_probe_peak(int kind, void* stream, double* flops) {
-  if (!flops || kind < 0 || kind > 2) return fail(TOGB_ERR_INVALID, "bad probe arguments");
-  cudaError_t e = togb::probe_peak(kind, (cudaStream_t)stream, flops);
+  if (!flops || kind < 0 || kind > 3) return fail(TOGB_ERR_INVALID, "bad probe arguments");
+  cudaError_t e = kind == 3 ? togb::probe_umma((cudaStream_t)stream, flops)
+                            : togb::probe_peak(kind, (cudaStream_t)stream, flops);
   if (e != cudaSuccess) return cuda_fail(e, "peak probe");
   return TOGB_OK;
 }

@@ -466,7 +466,79 @@ cudaError_t launch_bn(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorM
   return cudaGetLastError();
 }
 
+// Tensor-pipe probe: one CTA per SM issues back-to-back kind::tf32 MMAs
+// (M=128, N=256, K=8) from a zeroed shared-memory tile into tensor memory.
+__global__ void __launch_bounds__(128, 1) k_probe_umma(int iters, int32_t* err) {
+  extern __shared__ unsigned char dyn_raw[];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_sh;
+  unsigned char* smem = (unsigned char*)(((uintptr_t)dyn_raw + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x;
+  for (int i = tid; i < (16384 + 32768) / 16; i += blockDim.x) reinterpret_cast<float4*>(smem)[i] = make_float4(0, 0, 0, 0);
+  if (tid == 0) {
+    mbar_init(smem_u32(&mbar), 1);
+    fence_mbar_init();
+  }
+  if (tid < 32) {
+    tmem_alloc(smem_u32(&tmem_sh), 256);
+    tmem_relinquish();
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_sh;
+  bool ok = true;
+  if (tid == 0) {
+    const uint32_t a = smem_u32(smem), b = a + 16384;
+    constexpr uint32_t idesc = idesc_tf32(128, 256);
+    for (int it = 0; it < iters; ++it)
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+        umma_tf32(tmem, smem_desc_sw128(a + 32 * t), smem_desc_sw128(b + 32 * t), idesc, (it | t) ? 1u : 0u);
+    umma_commit(smem_u32(&mbar));
+    ok = mbar_wait_bounded(smem_u32(&mbar), 0);
+    if (!ok && err) atomicExch(err, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (tid < 32) tmem_dealloc(tmem, 256);
+}
+
 }  // namespace
+
+cudaError_t probe_umma(cudaStream_t st, double* flops) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int dyn = 16384 + 32768 + 1024;
+  cudaError_t e = cudaFuncSetAttribute(k_probe_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+  if (e != cudaSuccess) return e;
+  int32_t* err = nullptr;
+  if ((e = cudaMalloc(&err, 4)) != cudaSuccess) return e;
+  cudaMemsetAsync(err, 0, 4, st);
+  const int iters = 4096;
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  for (int rep = 0; rep < 2; ++rep) {
+    cudaEventRecord(t0, st);
+    k_probe_umma<<<sms, 128, dyn, st>>>(iters, err);
+    cudaEventRecord(t1, st);
+  }
+  e = cudaEventSynchronize(t1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, t0, t1);
+  int32_t herr = 0;
+  cudaMemcpy(&herr, err, 4, cudaMemcpyDeviceToHost);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaFree(err);
+  if (e != cudaSuccess) return e;
+  if (herr) return cudaErrorLaunchTimeout;
+  *flops = (double)sms * iters * 4 * 2.0 * 128 * 256 * 8 / (ms * 1e-3);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_umma(const JoinDesc& jd, const CUtensorMap* ta, const CUtensorMap* tb, const int64_t* s0,
                         int nslices, cudaStream_t st) {

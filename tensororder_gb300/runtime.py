@@ -69,8 +69,10 @@ EXPORTS = [
     "togb_version", "togb_last_error", "togb_program_create", "togb_program_info_get",
     "togb_program_reset", "togb_program_run", "togb_program_result", "togb_program_set_timing",
     "togb_program_join_times", "togb_program_destroy", "togb_tensordot_f64", "togb_probe_peak",
-    "togb_contract_static_f64",
+    "togb_contract_static_f64", "togb_program_joins",
 ]
+
+KERNEL_NAMES = {0: "direct", 1: "tiled", 2: "reduce", 3: "tensor"}
 
 STATIC_SCRATCH_BYTES = 32 << 20
 
@@ -104,6 +106,7 @@ def lib():
                                      _i32p, _i32p, c_void, c_void]
     L.togb_probe_peak.argtypes = [ctypes.c_int, c_void, ctypes.POINTER(ctypes.c_double)]
     L.togb_contract_static_f64.argtypes = [ctypes.POINTER(ProgramDesc), c_void, c_void, c_void]
+    L.togb_program_joins.argtypes = [c_void, ctypes.c_int, _i32p, ctypes.c_int32]
     for name in EXPORTS:
         if name not in ("togb_version", "togb_last_error", "togb_program_destroy"):
             getattr(L, name).restype = ctypes.c_int
@@ -206,6 +209,13 @@ class DeviceProgram:
         out = (ctypes.c_float * n)()
         check(lib().togb_program_join_times(self._h, out, n))
         return np.array(out, dtype=np.float64)
+
+    def joins(self, mode):
+        """Per join: (log2 M, log2 N, log2 K, kernel id) as an int array [joins, 4]."""
+        n = int(self.info.num_joins)
+        out = np.zeros((max(n, 1), 4), dtype=np.int32)
+        check(lib().togb_program_joins(self._h, int(mode), out.ctypes.data_as(_i32p), n))
+        return out[:n]
 
     def close(self):
         if getattr(self, "_h", None):
