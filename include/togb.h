@@ -68,16 +68,23 @@ typedef struct {
   const int32_t* group_edges;
 } togb_program_desc;
 
+/* Joins whose subtree reads no sliced edge compute the same tensor for every
+ * slice; they run once per togb_program_run call ("once" joins) and every
+ * slice reads their output.  The other joins run for every slice. */
 typedef struct {
   int64_t num_slices;
   int32_t num_joins;
   int32_t max_rank;              /* largest tensor rank over unsliced axes     */
   int32_t root_rank;             /* rank of the final tensor (0 for a count)   */
   int32_t num_launches;          /* kernel launches per chunk of slices        */
-  double flops_per_slice;        /* sum over joins of 2*M*N*K                  */
-  double bytes_per_slice_f64;    /* sum over joins of 8*(M*K + K*N + M*N)      */
+  double flops_per_slice;        /* per-slice joins: sum of 2*M*N*K            */
+  double bytes_per_slice_f64;    /* per-slice joins: sum of 8*(M*K + K*N + M*N) */
   int64_t workspace_per_slice[2];/* workspace bytes per slice, by togb_mode    */
   int64_t workspace_fixed[2];    /* workspace bytes independent of slice count */
+  int32_t num_joins_once;        /* slice-invariant joins                      */
+  int32_t pad_;
+  double flops_once;             /* slice-invariant joins: sum of 2*M*N*K      */
+  double bytes_once_f64;         /* slice-invariant joins: sum of 8*(M*K+K*N+M*N) */
 } togb_program_info;
 
 /* Lower and plan a program for `device`; copies the leaves to the device. */
@@ -101,9 +108,10 @@ togb_status togb_program_run(togb_program* prog, int mode, int64_t slice_begin, 
  * together with the compensation terms (`comp`, may be NULL). */
 togb_status togb_program_result(togb_program* prog, void* stream, double* out, double* comp, int64_t n);
 
-/* Per join in post-order, four int32: log2 M, log2 N, log2 K over unsliced
- * axes and the kernel used in `mode` (0 thread-per-output, 1 tiled SIMT GEMM,
- * 2 CTA-per-output reduction, 3 tensor-core GEMM).  n = num_joins. */
+/* Per join in post-order, five int32: log2 M, log2 N, log2 K over unsliced
+ * axes, the kernel used in `mode` (0 thread-per-output, 1 tiled SIMT GEMM,
+ * 2 CTA-per-output reduction, 3 tensor-core GEMM), and 1 when the join runs
+ * for every slice or 0 when it runs once per call.  n = num_joins. */
 togb_status togb_program_joins(const togb_program* prog, int mode, int32_t* out, int32_t n);
 
 /* Per-join device time of the last run with togb_program_set_timing(prog, 1):

@@ -44,10 +44,10 @@ __device__ __forceinline__ int shift_from_max(uint32_t bits) {
 __device__ __forceinline__ float pow2f(int sh) { return __int_as_float((127 + sh) << 23); }
 
 __device__ __forceinline__ int op_shift(const OpDesc& o, int b) {
-  return o.max_ptr ? shift_from_max(o.max_ptr[b]) : o.leaf_shift;
+  return o.max_ptr ? shift_from_max(o.max_ptr[b * o.meta_step]) : o.leaf_shift;
 }
 
-__device__ __forceinline__ int op_exp(const OpDesc& o, int b) { return o.exp_ptr ? o.exp_ptr[b] : 0; }
+__device__ __forceinline__ int op_exp(const OpDesc& o, int b) { return o.exp_ptr ? o.exp_ptr[b * o.meta_step] : 0; }
 
 }  // namespace
 }  // namespace togb

@@ -39,14 +39,14 @@ struct OpDesc {
   int32_t n_slice_terms;  // leaves: number of sliced axes
   int32_t k_fast;         // loader hint: the operand's smallest stride lies on a k bit
   int32_t leaf_shift;     // split mode, leaves: power-of-two normaliser
-  int32_t pad_;
+  int32_t meta_step;      // split mode: 1 = per-slice exponent/max entries, 0 = one entry for every slice
   int64_t s_outer[TOGB_MAXBITS];
   int64_t s_k[TOGB_MAXBITS];
   int64_t dk[TOGB_MAXBITS];            // dep_k(k+1) - dep_k(k) when bit t is the lowest zero of k
   int32_t slice_shift[TOGB_MAXBITS];   // bit of the global slice index for sliced axis j
   int64_t slice_stride[TOGB_MAXBITS];
-  const int32_t* exp_ptr;    // split mode, intermediates: per-slice exponent [chunk]
-  const uint32_t* max_ptr;   // split mode, intermediates: per-slice max bits [chunk]
+  const int32_t* exp_ptr;    // split mode, intermediates: exponent, entry b * meta_step for slice b
+  const uint32_t* max_ptr;   // split mode, intermediates: max bits, entry b * meta_step for slice b
   const void* ptr_lo;        // split mode, leaves: FP32 residual (value - hi), same layout
   Runs r_outer;              // run form of s_outer
   Runs r_k;                  // run form of s_k

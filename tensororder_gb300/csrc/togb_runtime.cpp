@@ -60,8 +60,10 @@ struct Node {
   std::unordered_map<int, int64_t> stride;  // unsliced edge -> element stride
   int rank = 0;                  // number of unsliced axes
   std::vector<int> m_lsb, n_lsb, k_lsb;     // GEMM bit order, least significant first
-  int64_t off = -1;              // per-slice arena offset (elements), joins only
+  int64_t off = -1;              // arena offset (elements), joins only
   int kernel = togb::K_DIRECT;
+  bool dep = true;               // depends on the slice (reads a sliced leaf, directly or below)
+  int slot = -1;                 // joins: index among the joins of its phase (metadata row)
 };
 
 int64_t pow2(int r) { return int64_t(1) << r; }
@@ -125,6 +127,10 @@ struct togb_program {
   std::vector<Node> nodes;
   int root = -1;
   std::vector<int> joins;  // node ids in execution (post-)order
+  // Joins by phase, as indices into `joins`: slice-invariant joins run once per
+  // togb_program_run call (their subtrees read no sliced edge, so every slice
+  // would compute the same tensor); the rest run for every slice of a chunk.
+  std::vector<int> once, per;
   std::unordered_map<int, int> group_of_edge;
   // leaves
   std::vector<int> leaf_rank;
@@ -135,8 +141,10 @@ struct togb_program {
   float* d_leaf32 = nullptr;    // split mode: FP32 rounding of each leaf value
   float* d_leaf32lo = nullptr;  // split mode: value - hi, rounded to FP32
   // planning
-  int64_t arena = 0;  // per-slice elements
-  double flops = 0, bytes64 = 0;
+  int64_t arena = 0;       // per-slice elements (slice-dependent joins)
+  int64_t arena_once = 0;  // elements of the slice-invariant joins, shared by all slices
+  double flops = 0, bytes64 = 0;            // per slice, slice-dependent joins
+  double flops_once = 0, bytes64_once = 0;  // once per run, slice-invariant joins
   int max_rank = 0;
   // device state
   double* d_acc = nullptr;  // [2 * 2^root_rank]: sum then compensation
@@ -153,8 +161,10 @@ struct togb_program {
   std::vector<CUtensorMap> tmaps;  // per join: TMA maps of A and B (tensor-core joins with plain operands)
   std::vector<char> use_tma;
   RootDesc rd{};
-  uint32_t* d_max = nullptr;  // split mode max bits [joins][B] inside the workspace
+  uint32_t* d_max = nullptr;  // split mode max bits [per-slice joins][B] inside the workspace
   size_t max_bytes = 0;
+  uint32_t* d_max_once = nullptr;  // split mode max bits [slice-invariant joins]
+  size_t max_once_bytes = 0;
   std::map<int, cudaGraphExec_t> graphs;  // by chunk slice count
   bool use_graphs = true;
   bool timing = false;
@@ -165,13 +175,26 @@ namespace {
 
 size_t elem_size(int mode) { return mode == TOGB_MODE_F64 ? 8 : 4; }
 
+int64_t round256(int64_t x) { return (x + 255) / 256 * 256; }
+
+// Workspace layout, from a 256-byte aligned base:
+//   [slice-invariant arena][slice-invariant exponent + max bits]   (fixed part)
+//   [per-slice arena x B][per-slice exponent x B][per-slice max bits x B]
 int64_t ws_per_slice(const togb_program* p, int mode) {
   int64_t b = p->arena * (int64_t)elem_size(mode);
-  if (mode == TOGB_MODE_SPLIT) b += 8 * (int64_t)p->joins.size();  // exponent + max bits
+  if (mode == TOGB_MODE_SPLIT) b += 8 * (int64_t)p->per.size();  // exponent + max bits
   return b;
 }
 
-const int64_t kWsFixed = 256;  // alignment slack
+int64_t ws_once(const togb_program* p, int mode) {
+  int64_t b = round256(p->arena_once * (int64_t)elem_size(mode));
+  if (mode == TOGB_MODE_SPLIT) b += round256(8 * (int64_t)p->once.size());
+  return b;
+}
+
+const int64_t kWsSlack = 256;  // alignment slack
+
+int64_t ws_fixed(const togb_program* p, int mode) { return kWsSlack + ws_once(p, mode); }
 
 void clear_graphs(togb_program* p) {
   for (auto& kv : p->graphs) cudaGraphExecDestroy(kv.second);
@@ -210,9 +233,6 @@ void plan_join(togb_program* p, Node& J) {
   for (size_t i = 0; i < J.m_lsb.size(); ++i) J.stride[J.m_lsb[i]] = pow2(nb + (int)i);
   const int mb = (int)J.m_lsb.size(), kb = (int)J.k_lsb.size();
   J.kernel = choose_kernel(mb, nb, kb);
-  const double M = std::ldexp(1.0, mb), N = std::ldexp(1.0, nb), K = std::ldexp(1.0, kb);
-  p->flops += 2.0 * M * N * K;
-  p->bytes64 += 8.0 * (M * K + K * N + M * N);
 }
 
 // Top-down layout requests.  A GEMM-shaped join (tiled / tensor-core kernels)
@@ -267,8 +287,10 @@ void plan_layouts(togb_program* p) {
   }
 }
 
-// First-fit arena over the join outputs, freeing operands after their consumer.
-void plan_arena(togb_program* p) {
+// First-fit arena over the outputs of one phase's joins, freeing an operand
+// after its consumer when both belong to the phase.  A slice-invariant output
+// read by a per-slice join stays live for the whole run.
+int64_t plan_phase_arena(togb_program* p, bool dep) {
   std::vector<std::pair<int64_t, int64_t>> live;  // (offset, size), sorted by offset
   int64_t top = 0;
   auto alloc = [&](int64_t size) {
@@ -288,12 +310,35 @@ void plan_arena(togb_program* p) {
   };
   for (int id : p->joins) {
     Node& J = p->nodes[id];
+    if (J.dep != dep) continue;
     const int64_t size = (pow2(J.rank) + kAlignElems - 1) / kAlignElems * kAlignElems;
     J.off = alloc(size);
-    for (int opnd : {J.left, J.right})
-      if (p->nodes[opnd].leaf < 0) release(p->nodes[opnd].off);
+    for (int opnd : {J.left, J.right}) {
+      const Node& O = p->nodes[opnd];
+      if (O.leaf < 0 && O.dep == dep) release(O.off);
+    }
   }
-  p->arena = std::max<int64_t>(top, kAlignElems);
+  return top;
+}
+
+void plan_arena(togb_program* p) {
+  p->once.clear();
+  p->per.clear();
+  p->flops = p->bytes64 = p->flops_once = p->bytes64_once = 0;
+  for (size_t j = 0; j < p->joins.size(); ++j) {
+    Node& J = p->nodes[p->joins[j]];
+    std::vector<int>& phase = J.dep ? p->per : p->once;
+    J.slot = (int)phase.size();
+    phase.push_back((int)j);
+    const Node& L = p->nodes[J.left];
+    const Node& R = p->nodes[J.right];
+    const int kb = (int)J.k_lsb.size();
+    const double M = std::ldexp(1.0, L.rank - kb), N = std::ldexp(1.0, R.rank - kb), K = std::ldexp(1.0, kb);
+    (J.dep ? p->flops : p->flops_once) += 2.0 * M * N * K;
+    (J.dep ? p->bytes64 : p->bytes64_once) += 8.0 * (M * K + K * N + M * N);
+  }
+  p->arena = std::max<int64_t>(plan_phase_arena(p, true), kAlignElems);
+  p->arena_once = plan_phase_arena(p, false);
 }
 
 // dep_k(k) for the first 16 values of k (the unrolled small-K kernels).
@@ -315,10 +360,35 @@ int is_natural(const JoinDesc& jd) {
   return jd.c_batch_stride == pow2(jd.mb + jd.nb) ? 1 : 0;
 }
 
+// Workspace regions for a chunk of B slices (see ws_per_slice / ws_once).
+struct WsLayout {
+  char* once;             // slice-invariant arena
+  int32_t* once_exp;      // [once joins]
+  uint32_t* once_max;     // [once joins]
+  char* per;              // per-slice arena, node j at per + off * B * es
+  int32_t* per_exp;       // [per joins][B]
+  uint32_t* per_max;      // [per joins][B]
+};
+
+WsLayout ws_layout(const togb_program* p, int mode, char* ws, int B) {
+  const int64_t es = (int64_t)elem_size(mode);
+  WsLayout w{};
+  w.once = ws;
+  char* meta = ws + round256(p->arena_once * es);
+  w.once_exp = (int32_t*)meta;
+  w.once_max = (uint32_t*)(meta + 4 * (int64_t)p->once.size());
+  w.per = ws + ws_once(p, mode);
+  char* pmeta = w.per + p->arena * (int64_t)B * es;
+  w.per_exp = (int32_t*)pmeta;
+  w.per_max = (uint32_t*)(pmeta + 4 * (int64_t)p->per.size() * B);
+  return w;
+}
+
 void fill_operand(const togb_program* p, const Node& X, const std::vector<int>& outer,
                   const std::vector<int>& k, int mode, char* ws, int B, OpDesc& od) {
   std::memset(&od, 0, sizeof(od));
   const size_t es = elem_size(mode);
+  const WsLayout w = ws_layout(p, mode, ws, B);
   if (X.leaf >= 0) {
     const char* base = mode == TOGB_MODE_F64 ? (const char*)p->d_leaf64 : (const char*)p->d_leaf32;
     od.ptr = base + p->leaf_off[X.leaf] * es;
@@ -336,13 +406,22 @@ void fill_operand(const togb_program* p, const Node& X, const std::vector<int>& 
     od.n_slice_terms = nt;
     od.leaf_shift = p->leaf_shift[X.leaf];
     if (mode == TOGB_MODE_SPLIT) od.ptr_lo = p->d_leaf32lo + p->leaf_off[X.leaf];
-  } else {
-    od.ptr = ws + X.off * (int64_t)B * es;
+  } else if (X.dep) {
+    od.ptr = w.per + X.off * (int64_t)B * es;
     od.batch_stride = pow2(X.rank);
     if (mode == TOGB_MODE_SPLIT) {
-      char* meta = ws + p->arena * (int64_t)B * es;
-      od.exp_ptr = (const int32_t*)(meta) + (int64_t)X.join * B;
-      od.max_ptr = (const uint32_t*)(meta + 4 * (int64_t)p->joins.size() * B) + (int64_t)X.join * B;
+      od.exp_ptr = w.per_exp + (int64_t)X.slot * B;
+      od.max_ptr = w.per_max + (int64_t)X.slot * B;
+      od.meta_step = 1;
+    }
+  } else {
+    // Slice-invariant intermediate: one tensor read by every slice.
+    od.ptr = w.once + X.off * (int64_t)es;
+    od.batch_stride = 0;
+    if (mode == TOGB_MODE_SPLIT) {
+      od.exp_ptr = w.once_exp + X.slot;
+      od.max_ptr = w.once_max + X.slot;
+      od.meta_step = 0;
     }
   }
   od.outer_bits = (int)outer.size();
@@ -445,7 +524,9 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
     jd.nb = (int)J.n_lsb.size();
     jd.kb = (int)J.k_lsb.size();
     jd.join = (int)j;
-    jd.c_ptr = ws + J.off * (int64_t)B * es;
+    const WsLayout w = ws_layout(p, mode, ws, B);
+    // A slice-invariant join runs once (one slice in its launch), into the shared arena.
+    jd.c_ptr = J.dep ? w.per + J.off * (int64_t)B * es : w.once + J.off * (int64_t)es;
     jd.c_batch_stride = pow2(J.rank);
     for (int i = 0; i < jd.mb; ++i) jd.c_s_m[i] = J.stride.at(J.m_lsb[i]);
     for (int i = 0; i < jd.nb; ++i) jd.c_s_n[i] = J.stride.at(J.n_lsb[i]);
@@ -456,9 +537,8 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
     jd.c_natural = is_natural(jd);
     jd.err = p->d_err;
     if (mode == TOGB_MODE_SPLIT) {
-      char* meta = ws + p->arena * (int64_t)B * es;
-      jd.c_exp = (int32_t*)meta + (int64_t)j * B;
-      jd.c_max = (uint32_t*)(meta + 4 * (int64_t)p->joins.size() * B) + (int64_t)j * B;
+      jd.c_exp = J.dep ? w.per_exp + (int64_t)J.slot * B : w.once_exp + J.slot;
+      jd.c_max = J.dep ? w.per_max + (int64_t)J.slot * B : w.once_max + J.slot;
       // The tensor-core kernel tiles 128 rows of M: put the larger extent there.
       if (split_kernel(p, J) == togb::K_UMMA) {
         if (jd.mb < 7 && jd.nb > jd.mb) swap_operands(jd);
@@ -474,32 +554,90 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
   p->rd.acc_sum = p->d_acc;
   p->rd.acc_comp = p->d_acc + pow2(Rn.rank);
   if (mode == TOGB_MODE_SPLIT) {
-    p->d_max = (uint32_t*)(ws + p->arena * (int64_t)B * es + 4 * (int64_t)p->joins.size() * B);
-    p->max_bytes = 4 * p->joins.size() * (size_t)B;
+    const WsLayout w = ws_layout(p, mode, ws, B);
+    p->d_max = w.per_max;
+    p->max_bytes = 4 * p->per.size() * (size_t)B;
+    p->d_max_once = w.once_max;
+    p->max_once_bytes = 4 * p->once.size();
   } else {
-    p->d_max = nullptr;
-    p->max_bytes = 0;
+    p->d_max = p->d_max_once = nullptr;
+    p->max_bytes = p->max_once_bytes = 0;
   }
 }
 
-togb_status enqueue_chunk(togb_program* p, int mode, int nb, cudaStream_t st,
+// Queue one phase: the slice-invariant joins once (`once`, one slice per
+// launch), or the per-slice joins and the root reduction for a chunk of `nb`
+// slices.  With `ev`, event i is recorded before the phase's join i and one
+// more after its last join.
+togb_status enqueue_phase(togb_program* p, int mode, bool once, int nb, cudaStream_t st,
                           std::vector<cudaEvent_t>* ev) {
-  // Split mode: every output's per-slice maximum starts at +0 (atomicMax target).
-  if (p->max_bytes) TOGB_CUDA(cudaMemsetAsync(p->d_max, 0, p->max_bytes, st));
-  for (size_t j = 0; j < p->joins.size(); ++j) {
-    if (ev) TOGB_CUDA(cudaEventRecord((*ev)[j], st));
+  const std::vector<int>& js = once ? p->once : p->per;
+  // Split mode: every output's maximum starts at +0 (atomicMax target).
+  uint32_t* mx = once ? p->d_max_once : p->d_max;
+  const size_t mx_bytes = once ? p->max_once_bytes : p->max_bytes;
+  if (mx_bytes) TOGB_CUDA(cudaMemsetAsync(mx, 0, mx_bytes, st));
+  const int launch_slices = once ? 1 : nb;
+  for (size_t i = 0; i < js.size(); ++i) {
+    const int j = js[i];
+    if (ev) TOGB_CUDA(cudaEventRecord((*ev)[i], st));
     const Node& J = p->nodes[p->joins[j]];
     const int kernel = mode == TOGB_MODE_SPLIT ? split_kernel(p, J) : J.kernel;
     cudaError_t e;
     if (kernel == togb::K_UMMA && mode == TOGB_MODE_SPLIT && p->use_tma[j])
-      e = togb::launch_umma(p->jds[j], &p->tmaps[2 * j], &p->tmaps[2 * j + 1], p->d_s0, nb, st);
+      e = togb::launch_umma(p->jds[j], &p->tmaps[2 * j], &p->tmaps[2 * j + 1], p->d_s0, launch_slices, st);
     else
-      e = togb::launch_join(mode, kernel, p->jds[j], p->d_s0, nb, st);
+      e = togb::launch_join(mode, kernel, p->jds[j], p->d_s0, launch_slices, st);
     if (e != cudaSuccess) return cuda_fail(e, "join kernel launch");
   }
-  if (ev) TOGB_CUDA(cudaEventRecord((*ev)[p->joins.size()], st));
+  if (ev) TOGB_CUDA(cudaEventRecord((*ev)[js.size()], st));
+  if (once) return TOGB_OK;
   cudaError_t e = togb::launch_root(mode, p->rd, p->d_s0, nb, st);
   if (e != cudaSuccess) return cuda_fail(e, "root kernel launch");
+  return TOGB_OK;
+}
+
+// Queue a phase on `st`: timed launch by launch when timing is on (adding
+// each join's device time to join_ms), else as a CUDA graph captured once per
+// (phase, chunk size) and replayed.
+togb_status run_phase(togb_program* p, int mode, bool once, int nb, cudaStream_t st) {
+  const std::vector<int>& js = once ? p->once : p->per;
+  if (once && js.empty()) return TOGB_OK;
+  if (p->timing) {
+    std::vector<cudaEvent_t> ev(js.size() + 1, nullptr);
+    togb_status r = TOGB_OK;
+    for (auto& x : ev)
+      if (cudaEventCreate(&x) != cudaSuccess) { x = nullptr; r = fail(TOGB_ERR_CUDA, "event create"); }
+    if (r == TOGB_OK) r = enqueue_phase(p, mode, once, nb, st, &ev);
+    if (r == TOGB_OK) {
+      cudaError_t e = cudaEventSynchronize(ev.back());
+      for (size_t i = 0; e == cudaSuccess && i < js.size(); ++i) {
+        float ms = 0;
+        e = cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+        p->join_ms[js[i]] += ms;
+      }
+      if (e != cudaSuccess) r = cuda_fail(e, "join timing");
+    }
+    for (auto& x : ev)
+      if (x) cudaEventDestroy(x);
+    return r;
+  }
+  if (!p->use_graphs) return enqueue_phase(p, mode, once, nb, st, nullptr);
+  const int key = once ? -1 : nb;
+  auto it = p->graphs.find(key);
+  if (it == p->graphs.end()) {
+    cudaGraph_t g = nullptr;
+    TOGB_CUDA(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
+    togb_status r = enqueue_phase(p, mode, once, nb, p->cap_stream, nullptr);
+    cudaError_t ce = cudaStreamEndCapture(p->cap_stream, &g);
+    if (r != TOGB_OK) { if (g) cudaGraphDestroy(g); return r; }
+    if (ce != cudaSuccess) return cuda_fail(ce, "graph capture");
+    cudaGraphExec_t ex = nullptr;
+    ce = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return cuda_fail(ce, "graph instantiate");
+    it = p->graphs.emplace(key, ex).first;
+  }
+  TOGB_CUDA(cudaGraphLaunch(it->second, st));
   return TOGB_OK;
 }
 
@@ -574,10 +712,11 @@ togb_status lower_host(const togb_program_desc* d, int device, togb_program** ou
       used[tok] = 1;
       Node n;
       n.leaf = tok;
+      n.dep = false;
       const std::vector<int>& axes = p->leaf_axes[tok];
       const int R = (int)axes.size();
       for (int a = 0; a < R; ++a) {
-        if (p->group_of_edge.count(axes[a])) continue;
+        if (p->group_of_edge.count(axes[a])) { n.dep = true; continue; }
         if (n.stride.count(axes[a])) { delete p; return fail(TOGB_ERR_INVALID, "repeated edge in a leaf"); }
         n.ref.push_back(axes[a]);
         n.stride[axes[a]] = pow2(R - 1 - a);
@@ -591,6 +730,7 @@ togb_status lower_host(const togb_program_desc* d, int device, togb_program** ou
       n.right = stack.back(); stack.pop_back();
       n.left = stack.back(); stack.pop_back();
       n.join = (int)p->joins.size();
+      n.dep = p->nodes[n.left].dep || p->nodes[n.right].dep;
       p->nodes.push_back(std::move(n));
       const int id = (int)p->nodes.size() - 1;
       plan_join(p, p->nodes[id]);
@@ -603,6 +743,11 @@ togb_status lower_host(const togb_program_desc* d, int device, togb_program** ou
   for (int l = 0; l < d->num_leaves; ++l)
     if (!used[l]) { delete p; return fail(TOGB_ERR_INVALID, "leaf never pushed"); }
   p->root = stack[0];
+  // Unsliced programs have one slice: nothing to hoist.  The root always runs
+  // per slice (it feeds the slice sum).
+  if (p->G == 0)
+    for (Node& n : p->nodes) n.dep = true;
+  p->nodes[p->root].dep = true;
   for (const Node& n : p->nodes) p->max_rank = std::max(p->max_rank, n.rank);
   plan_layouts(p);
   plan_arena(p);
@@ -659,13 +804,16 @@ togb_status togb_program_info_get(const togb_program* p, togb_program_info* info
   info->num_joins = (int32_t)p->joins.size();
   info->max_rank = p->max_rank;
   info->root_rank = p->nodes[p->root].rank;
-  info->num_launches = (int32_t)p->joins.size() + 1;
+  info->num_launches = (int32_t)p->per.size() + 1;
   info->flops_per_slice = p->flops;
   info->bytes_per_slice_f64 = p->bytes64;
   for (int m = 0; m < 2; ++m) {
     info->workspace_per_slice[m] = ws_per_slice(p, m);
-    info->workspace_fixed[m] = kWsFixed;
+    info->workspace_fixed[m] = ws_fixed(p, m);
   }
+  info->num_joins_once = (int32_t)p->once.size();
+  info->flops_once = p->flops_once;
+  info->bytes_once_f64 = p->bytes64_once;
   return TOGB_OK;
 }
 
@@ -682,10 +830,11 @@ togb_status togb_program_joins(const togb_program* p, int mode, int32_t* out, in
   if (n != (int32_t)p->joins.size()) return fail(TOGB_ERR_INVALID, "n must equal the number of joins");
   for (size_t j = 0; j < p->joins.size(); ++j) {
     const Node& J = p->nodes[p->joins[j]];
-    out[4 * j + 0] = (int32_t)J.m_lsb.size();
-    out[4 * j + 1] = (int32_t)J.n_lsb.size();
-    out[4 * j + 2] = (int32_t)J.k_lsb.size();
-    out[4 * j + 3] = mode == TOGB_MODE_SPLIT ? split_kernel(p, J) : J.kernel;
+    out[5 * j + 0] = (int32_t)J.m_lsb.size();
+    out[5 * j + 1] = (int32_t)J.n_lsb.size();
+    out[5 * j + 2] = (int32_t)J.k_lsb.size();
+    out[5 * j + 3] = mode == TOGB_MODE_SPLIT ? split_kernel(p, J) : J.kernel;
+    out[5 * j + 4] = J.dep ? 1 : 0;
   }
   return TOGB_OK;
 }
@@ -713,14 +862,15 @@ togb_status togb_program_run(togb_program* p, int mode, int64_t begin, int64_t e
   cudaStream_t st = (cudaStream_t)stream_v;
   TOGB_CUDA(cudaSetDevice(p->device));
   const int64_t per = ws_per_slice(p, mode);
+  const int64_t fixed = ws_fixed(p, mode);
   const int64_t want = end - begin;
   if (!workspace) {
     // Own workspace: as many slices per chunk as fit a quarter of free memory.
     size_t freeb = 0, totalb = 0;
     TOGB_CUDA(cudaMemGetInfo(&freeb, &totalb));
-    int64_t fit = (int64_t)(freeb / 4 + p->own_ws_bytes) / per;
+    int64_t fit = ((int64_t)(freeb / 4 + p->own_ws_bytes) - fixed) / per;
     int64_t B = std::max<int64_t>(1, std::min<int64_t>(want, std::min<int64_t>(fit, 65535)));
-    const size_t need = (size_t)(B * per + kWsFixed);
+    const size_t need = (size_t)(B * per + fixed);
     if (p->own_ws_bytes < need) {
       if (p->own_ws) { cudaFree(p->own_ws); p->own_ws = nullptr; p->own_ws_bytes = 0; }
       cudaError_t e = cudaMalloc(&p->own_ws, need);
@@ -731,7 +881,7 @@ togb_status togb_program_run(togb_program* p, int mode, int64_t begin, int64_t e
     ws_bytes = p->own_ws_bytes;
   }
   char* ws = (char*)(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
-  const int64_t usable = (int64_t)ws_bytes - (int64_t)(ws - (char*)workspace);
+  const int64_t usable = (int64_t)ws_bytes - (int64_t)(ws - (char*)workspace) - ws_once(p, mode);
   int64_t B = usable > 0 ? usable / per : 0;
   B = std::min<int64_t>(B, std::min<int64_t>(want, 65535));
   if (B < 1) return fail(TOGB_ERR_OOM, "workspace smaller than one slice");
@@ -742,47 +892,16 @@ togb_status togb_program_run(togb_program* p, int mode, int64_t begin, int64_t e
     p->cur_B = (int)B;
     p->cur_ws = ws;
   }
-  std::vector<cudaEvent_t> ev;
-  if (p->timing) {
-    ev.resize(p->joins.size() + 1);
-    for (auto& x : ev) TOGB_CUDA(cudaEventCreate(&x));
-    p->join_ms.assign(p->joins.size(), 0.f);
-  }
-  for (int64_t s = begin; s < end; s += B) {
+  if (p->timing) p->join_ms.assign(p->joins.size(), 0.f);
+  // The slice-invariant joins first (once per call), then every chunk.
+  togb_status r = run_phase(p, mode, true, 1, st);
+  for (int64_t s = begin; r == TOGB_OK && s < end; s += B) {
     const int nb = (int)std::min<int64_t>(B, end - s);
     cudaError_t e = togb::launch_set_s0(p->d_s0, s, st);
     if (e != cudaSuccess) return cuda_fail(e, "slice base update");
-    if (p->timing || !p->use_graphs) {
-      togb_status r = enqueue_chunk(p, mode, nb, st, p->timing ? &ev : nullptr);
-      if (r != TOGB_OK) return r;
-      if (p->timing) {
-        TOGB_CUDA(cudaEventSynchronize(ev.back()));
-        for (size_t j = 0; j < p->joins.size(); ++j) {
-          float ms = 0;
-          TOGB_CUDA(cudaEventElapsedTime(&ms, ev[j], ev[j + 1]));
-          p->join_ms[j] += ms;
-        }
-      }
-      continue;
-    }
-    auto it = p->graphs.find(nb);
-    if (it == p->graphs.end()) {
-      cudaGraph_t g = nullptr;
-      TOGB_CUDA(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
-      togb_status r = enqueue_chunk(p, mode, nb, p->cap_stream, nullptr);
-      cudaError_t ce = cudaStreamEndCapture(p->cap_stream, &g);
-      if (r != TOGB_OK) { if (g) cudaGraphDestroy(g); return r; }
-      if (ce != cudaSuccess) return cuda_fail(ce, "graph capture");
-      cudaGraphExec_t ex = nullptr;
-      ce = cudaGraphInstantiate(&ex, g, 0);
-      cudaGraphDestroy(g);
-      if (ce != cudaSuccess) return cuda_fail(ce, "graph instantiate");
-      it = p->graphs.emplace(nb, ex).first;
-    }
-    TOGB_CUDA(cudaGraphLaunch(it->second, st));
+    r = run_phase(p, mode, false, nb, st);
   }
-  for (auto& x : ev) cudaEventDestroy(x);
-  return TOGB_OK;
+  return r;
 }
 
 togb_status togb_program_result(togb_program* p, void* stream, double* out, double* comp, int64_t n) {
@@ -900,7 +1019,8 @@ togb_status togb_probe_peak(int kind, void* stream, double* flops) {
 // Contraction of a whole program in FP64 with every intermediate inside a
 // caller-supplied scratch region (the library's static device array).  Layout:
 // [slice base, 256 B][accumulator: 2 * 2^root_rank doubles, rounded up to
-// 256 B][arena: per-slice arena * chunk].  No device memory is allocated.
+// 256 B][workspace: slice-invariant part, then per-slice part * chunk].  No
+// device memory is allocated.
 togb_status togb::static_contract_f64(const togb_program_desc* d, const double* d_leaf, char* scratch,
                                       size_t scratch_bytes, double* d_out, cudaStream_t st) {
   togb_program* p = nullptr;
@@ -909,15 +1029,16 @@ togb_status togb::static_contract_f64(const togb_program_desc* d, const double* 
   if (r != TOGB_OK) return r;
   const int64_t E = pow2(p->nodes[p->root].rank);
   const int64_t head = 256 + (2 * E * 8 + 255) / 256 * 256;
-  const int64_t per = p->arena * 8;
-  if (head + per > (int64_t)scratch_bytes) {
-    const std::string msg = "program needs " + std::to_string(head + per) +
+  const int64_t per = ws_per_slice(p, TOGB_MODE_F64);
+  const int64_t once = ws_once(p, TOGB_MODE_F64);
+  if (head + once + per > (int64_t)scratch_bytes) {
+    const std::string msg = "program needs " + std::to_string(head + once + per) +
                             " bytes of device scratch for one slice; the static scratch holds " +
                             std::to_string(scratch_bytes) + " bytes";
     delete p;
     return fail(TOGB_ERR_OOM, msg);
   }
-  const int64_t B = std::min<int64_t>({((int64_t)scratch_bytes - head) / per, p->num_slices, 65535});
+  const int64_t B = std::min<int64_t>({((int64_t)scratch_bytes - head - once) / per, p->num_slices, 65535});
   p->d_leaf64 = const_cast<double*>(d_leaf);
   p->d_s0 = (int64_t*)scratch;
   p->d_acc = (double*)(scratch + 256);
@@ -926,11 +1047,12 @@ togb_status togb::static_contract_f64(const togb_program_desc* d, const double* 
   togb_status out = TOGB_OK;
   cudaError_t e = cudaMemsetAsync(p->d_acc, 0, 2 * E * 8, st);
   if (e != cudaSuccess) out = cuda_fail(e, "accumulator clear");
+  if (out == TOGB_OK) out = enqueue_phase(p, TOGB_MODE_F64, true, 1, st, nullptr);
   for (int64_t s = 0; out == TOGB_OK && s < p->num_slices; s += B) {
     const int nb = (int)std::min<int64_t>(B, p->num_slices - s);
     e = togb::launch_set_s0(p->d_s0, s, st);
     if (e != cudaSuccess) { out = cuda_fail(e, "slice base update"); break; }
-    out = enqueue_chunk(p, TOGB_MODE_F64, nb, st, nullptr);
+    out = enqueue_phase(p, TOGB_MODE_F64, false, nb, st, nullptr);
   }
   if (out == TOGB_OK && (e = togb::launch_finalize(p->d_acc, E, d_out, st)) != cudaSuccess)
     out = cuda_fail(e, "result write");

@@ -48,6 +48,10 @@ class ProgramInfo(ctypes.Structure):
         ("bytes_per_slice_f64", ctypes.c_double),
         ("workspace_per_slice", ctypes.c_int64 * 2),
         ("workspace_fixed", ctypes.c_int64 * 2),
+        ("num_joins_once", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("flops_once", ctypes.c_double),
+        ("bytes_once_f64", ctypes.c_double),
     ]
 
 
@@ -211,9 +215,11 @@ class DeviceProgram:
         return np.array(out, dtype=np.float64)
 
     def joins(self, mode):
-        """Per join: (log2 M, log2 N, log2 K, kernel id) as an int array [joins, 4]."""
+        """Per join: (log2 M, log2 N, log2 K, kernel id, runs per slice) as an
+        int array [joins, 5]; the last column is 0 for slice-invariant joins,
+        which run once per call."""
         n = int(self.info.num_joins)
-        out = np.zeros((max(n, 1), 4), dtype=np.int32)
+        out = np.zeros((max(n, 1), 5), dtype=np.int32)
         check(lib().togb_program_joins(self._h, int(mode), out.ctypes.data_as(_i32p), n))
         return out[:n]
 
