@@ -97,6 +97,11 @@ cudaError_t launch_root(int mode, const RootDesc& rd, const int64_t* s0, int nsl
 // gather through the deposit layouts.
 cudaError_t launch_umma(const JoinDesc& jd, const CUtensorMap* ta, const CUtensorMap* tb, const int64_t* s0,
                         int nslices, cudaStream_t st);
+// Warp-specialised tensor-core GEMM over TMA-loaded operands (togb_umma_ws.cu).
+cudaError_t launch_umma_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorMap& tb, int nslices,
+                           cudaStream_t st);
+// Rows of the B-operand TMA box of launch_umma_ws for an N of 2^nb.
+int umma_ws_box_rows_b(int nb);
 cudaError_t launch_set_s0(int64_t* d_s0, int64_t value, cudaStream_t st);
 // out[e] = acc[e] + acc[E + e]: the compensated sum of a root accumulator.
 cudaError_t launch_finalize(const double* acc, int64_t E, double* out, cudaStream_t st);

@@ -453,14 +453,16 @@ int split_kernel(const togb_program* p, const Node& J) {
   return J.kernel;
 }
 
-// An intermediate operand stored as a row-major [rows][K] matrix per slice.
+// A split-form intermediate operand stored as a row-major [rows][K] matrix,
+// one per slice or one shared by all slices (slice-invariant).  Leaves (read
+// from their parent tensors) carry no exponent table and never qualify.
 bool plain_k_major(const OpDesc& o) {
-  if (o.batch_stride == 0) return false;  // leaf: read from its parent tensor
+  if (!o.exp_ptr) return false;
   for (int i = 0; i < o.k_bits; ++i)
     if (o.s_k[i] != pow2(i)) return false;
   for (int i = 0; i < o.outer_bits; ++i)
     if (o.s_outer[i] != pow2(o.k_bits + i)) return false;
-  return o.batch_stride == pow2(o.k_bits + o.outer_bits);
+  return o.batch_stride == 0 || o.batch_stride == pow2(o.k_bits + o.outer_bits);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -542,8 +544,10 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
       // The tensor-core kernel tiles 128 rows of M: put the larger extent there.
       if (split_kernel(p, J) == togb::K_UMMA) {
         if (jd.mb < 7 && jd.nb > jd.mb) swap_operands(jd);
+        const int sl_a = jd.a.batch_stride ? B : 1, sl_b = jd.b.batch_stride ? B : 1;
         p->use_tma[j] = plain_k_major(jd.a) && plain_k_major(jd.b) && jd.kb >= 2 &&
-                        make_tmap(jd.a, B, 128, &p->tmaps[2 * j]) && make_tmap(jd.b, B, 64, &p->tmaps[2 * j + 1]);
+                        make_tmap(jd.a, sl_a, 128, &p->tmaps[2 * j]) &&
+                        make_tmap(jd.b, sl_b, togb::umma_ws_box_rows_b(jd.nb), &p->tmaps[2 * j + 1]);
       }
     }
   }

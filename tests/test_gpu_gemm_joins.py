@@ -49,7 +49,8 @@ def make_program(seed, m, n, k, slices=0):
     return prog.validate()
 
 
-SHAPES = [(6, 6, 4), (7, 7, 5), (8, 7, 6), (6, 8, 7), (9, 6, 4), (7, 9, 8), (8, 8, 9), (6, 6, 10)]
+SHAPES = [(6, 6, 4), (7, 7, 5), (8, 7, 6), (6, 8, 7), (9, 6, 4), (7, 9, 8), (8, 8, 9), (6, 6, 10),
+          (7, 7, 4), (10, 8, 6), (7, 11, 6), (8, 12, 5), (9, 7, 11)]
 
 
 @pytest.mark.parametrize("m,n,k", SHAPES)
@@ -67,8 +68,11 @@ def test_gemm_join(m, n, k, mode, tol, cuda):
 
 
 @pytest.mark.parametrize("mode,tol", [(runtime.MODE_F64, 1e-12), (runtime.MODE_SPLIT, 1e-6)])
-def test_gemm_join_sliced(mode, tol, cuda):
-    prog = make_program(77, 7, 6, 5, slices=3)
+@pytest.mark.parametrize("shape", [(7, 6, 5, 3), (8, 8, 6, 2), (6, 9, 7, 2)])
+def test_gemm_join_sliced(shape, mode, tol, cuda):
+    """X is slice-invariant (computed once, read by every slice), Y per slice."""
+    m, n, k, g = shape
+    prog = make_program(77 + m + n + k, m, n, k, slices=g)
     want = sum(oracle.contract(prog, s)[0] for s in range(prog.num_slices))
     dp = runtime.DeviceProgram(prog)
     dp.reset()
