@@ -103,13 +103,29 @@ __device__ __forceinline__ void store_vec(double* p, const double* v) {
 }
 
 // Thread-per-output kernel: each thread computes VEC consecutive outputs in
-// the output's own address order (slice-major), recovering (m, n) from the
-// address with the inverse runs, so every store is a contiguous vector store
-// whatever order the consumer asked for; 2*VEC*K loads are in flight at once.
+// the output's own address order (slice-major), so every store is a
+// contiguous vector store whatever order the consumer asked for; 2*VEC*K
+// loads are in flight at once.  The operand offsets of an output address q
+// are sums of per-bit contributions (address bit -> m or n bit -> operand
+// stride), so each block tabulates them for q's four 6-bit digits in shared
+// memory: an output costs two table reads per operand, not a walk over the
+// bit runs of its layouts.
 template <int MODE, class T, int KK, int VEC>
 __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ JoinDesc jd,
                                                      const int64_t* __restrict__ d_s0, int nslices) {
+  __shared__ int32_t tabA[4][64], tabB[4][64];
   const int mnb = jd.mb + jd.nb;
+  const uint64_t nmask = (1ull << jd.nb) - 1;
+  const uint64_t mnmask = (1ull << mnb) - 1;
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    const int lvl = i >> 6;
+    const uint64_t q = ((uint64_t)(i & 63) << (6 * lvl)) & mnmask;
+    const uint64_t m = jd.c_natural ? (q >> jd.nb) : (uint64_t)dep(jd.r_inv_m, q);
+    const uint64_t n = jd.c_natural ? (q & nmask) : (uint64_t)dep(jd.r_inv_n, q);
+    tabA[lvl][i & 63] = (int32_t)dep(jd.a.r_outer, m);
+    tabB[lvl][i & 63] = (int32_t)dep(jd.b.r_outer, n);
+  }
+  __syncthreads();
   const int64_t groups = ((int64_t)nslices << mnb) / VEC;
   const int64_t groups_pad = (groups + 31) & ~(int64_t)31;
   const int64_t per_slice = (1ll << mnb) / VEC;  // groups per slice (power of two)
@@ -119,8 +135,6 @@ __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ Joi
   const T* __restrict__ A = (const T*)jd.a.ptr;
   const T* __restrict__ B = (const T*)jd.b.ptr;
   T* __restrict__ C = (T*)jd.c_ptr;
-  const uint64_t nmask = (1ull << jd.nb) - 1;
-  const uint64_t mnmask = (1ull << mnb) - 1;
   for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < groups_pad;
        g += (int64_t)gridDim.x * blockDim.x) {
     const bool valid = g < groups;
@@ -130,7 +144,17 @@ __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ Joi
     int sa = 0, sb = 0;
     if (valid) {
       const int64_t s = s0 + b;
-      const int64_t soa = slice_offset(jd.a, b, s), sob = slice_offset(jd.b, b, s);
+      const uint64_t q0 = (uint64_t)idx0 & mnmask;  // output address within the slice
+      int64_t soa = slice_offset(jd.a, b, s), sob = slice_offset(jd.b, b, s);
+      if (mnb > 24) {  // address bits above the tables
+        const uint64_t qh = q0 & ~((1ull << 24) - 1);
+        const uint64_t m = jd.c_natural ? (qh >> jd.nb) : (uint64_t)dep(jd.r_inv_m, qh);
+        const uint64_t n = jd.c_natural ? (qh & nmask) : (uint64_t)dep(jd.r_inv_n, qh);
+        soa += dep(jd.a.r_outer, m);
+        sob += dep(jd.b.r_outer, n);
+      }
+      soa += tabA[3][(q0 >> 18) & 63] + tabA[2][(q0 >> 12) & 63] + tabA[1][(q0 >> 6) & 63];
+      sob += tabB[3][(q0 >> 18) & 63] + tabB[2][(q0 >> 12) & 63] + tabB[1][(q0 >> 6) & 63];
       float fa = 1.f, fb = 1.f;
       if (MODE == 1) {
         sa = op_shift(jd.a, b);
@@ -141,12 +165,8 @@ __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ Joi
       T out[VEC];
 #pragma unroll
       for (int j = 0; j < VEC; ++j) {
-        const uint64_t q = (uint64_t)(idx0 + j) & mnmask;  // output address within the slice
-        const uint64_t m = jd.c_natural ? (q >> jd.nb) : (uint64_t)dep(jd.r_inv_m, q);
-        const uint64_t n = jd.c_natural ? (q & nmask) : (uint64_t)dep(jd.r_inv_n, q);
-        const int64_t oa = soa + dep(jd.a.r_outer, m);
-        const int64_t ob = sob + dep(jd.b.r_outer, n);
-        out[j] = dot_k<MODE, T, KK>(jd, A, B, oa, ob, K, fa, fb);
+        const int lo = (int)((q0 + j) & 63);  // VEC divides 64: the upper digits are shared
+        out[j] = dot_k<MODE, T, KK>(jd, A, B, soa + tabA[0][lo], sob + tabB[0][lo], K, fa, fb);
       }
       if (VEC == 4) {
         store_vec(C + idx0, out);  // program outputs are dense per slice: address = linear index
