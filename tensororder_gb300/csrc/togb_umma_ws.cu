@@ -21,10 +21,12 @@
 // small, main products last, and the read-out warps add the window into
 // round-to-nearest registers while the next window's MMAs run.
 //
-// The epilogue stages the tile in shared memory and writes it in the output's
-// own address order (row-major float4 stores when the output's lowest address
-// bits are the tile's n bits), then records the slice maximum and exponent
-// like the other split-form kernels.
+// The kernel is persistent (one CTA per SM walking the tiles), so the next
+// tile's loads, conversions and first MMAs overlap the current tile's
+// epilogue.  Each read-out thread owns one output row: it stores its columns
+// straight from registers (float4 stores when the output's lowest address bits
+// are the tile's n bits), then the slice maximum and exponent are recorded
+// like in the other split-form kernels.
 //
 // Operands that do not vary with the slice (slice-invariant intermediates) use
 // a tensor map with one slice and slice coordinate 0.  Every wait is bounded:
@@ -49,9 +51,7 @@ struct WsSmem {
   static constexpr int B_BYTES = BN * kBK * 4;
   static constexpr int RAW = A_BYTES + B_BYTES;  // TMA target, converted in place to hi
   static constexpr int STAGE = 2 * RAW;          // [hi: A | B][lo: A | B]
-  static constexpr int CROW = BN + 4;            // staging row stride of the output tile (floats)
   static constexpr int DYN = NST * STAGE + 1024;
-  static_assert(kBM * CROW * 4 <= NST * STAGE, "output staging tile fits in the stages");
   static_assert(DYN <= 227 * 1024, "shared memory budget");
 };
 
@@ -67,11 +67,27 @@ __device__ __forceinline__ void split4(float4 x, float f, float4& hi, float4& lo
   }
 }
 
+// Output tiles are numbered slice-major, n-tile fastest: consecutive tiles of
+// a CTA's neighbours share their A rows in L2.
+struct TileMap {
+  int tps_bits, tn_bits;
+  __device__ __forceinline__ void decode(int64_t t, int& b, uint64_t& m0, uint64_t& n0, int bn) const {
+    b = (int)(t >> tps_bits);
+    const uint64_t r = (uint64_t)t & ((1ull << tps_bits) - 1);
+    m0 = (r >> tn_bits) * kBM;
+    n0 = (r & ((1ull << tn_bits) - 1)) * (uint64_t)bn;
+  }
+};
+
+// Persistent: each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// The stage ring and the two accumulator sets run continuously across tiles,
+// so the next tile's loads, conversions and first MMAs overlap the current
+// tile's epilogue.
 template <int BN, int NST>
 __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant__ JoinDesc jd,
                                                           const __grid_constant__ CUtensorMap tmA,
                                                           const __grid_constant__ CUtensorMap tmB,
-                                                          int nslices, int tiles_n_bits) {
+                                                          int64_t ntiles, TileMap tm) {
   using L = WsSmem<BN, NST>;
   constexpr int HALF = BN / 2;        // columns per read-out warp
   constexpr uint32_t kCols = 2 * BN;  // two accumulator sets
@@ -82,21 +98,13 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
   __shared__ uint32_t tmem_sh;
   __shared__ int abort_sh;
   __shared__ int64_t tCm[kBM], tCn[BN];
-  __shared__ uint32_t red[kRead / 32];
 
-  const int b = blockIdx.y + blockIdx.z * gridDim.y;
-  if (b >= nslices) return;
   // After one CTA's wait expired the result is void: later CTAs leave at once.
   if (jd.err && *(volatile int32_t*)jd.err) return;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   unsigned char* smem = (unsigned char*)(((uintptr_t)dyn_raw + 1023) & ~(uintptr_t)1023);
   const uint32_t sbase = smem_u32(smem);
-  const uint64_t tile = blockIdx.x;
-  const uint64_t m0 = (tile >> tiles_n_bits) * kBM;
-  const uint64_t n0 = (tile & ((1ull << tiles_n_bits) - 1)) * BN;
   const int64_t M = 1ll << jd.mb, N = 1ll << jd.nb, K = 1ll << jd.kb;
-  const int mlim = (int)min((int64_t)kBM, M - (int64_t)m0);
-  const int nlim = (int)min((int64_t)BN, N - (int64_t)n0);
   const int ksteps = K >= 8 ? (int)(K / 8) : 1;  // MMA k-steps of 8
   const int nwin = (ksteps + 1) / 2;              // windows of two k-steps
   const int nchunks = (nwin + 1) / 2;             // TMA chunks of four k-steps
@@ -126,62 +134,68 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
   tc_fence_after();
   const uint32_t tmem = tmem_sh;
   volatile int* abort = &abort_sh;
-  const int sa = op_shift(jd.a, b), sb = op_shift(jd.b, b);
 
   if (warp == 0) {
     // ---------------------------------------------------------------- producer
     if (lane == 0) {
-      const int asl = jd.a.batch_stride ? b : 0, bsl = jd.b.batch_stride ? b : 0;
-      int issued = 0;
-      for (int c = 0; c < nchunks; ++c) {
-        const int st = c % NST, u = c / NST;
-        if (c >= NST && !mbar_wait_or_abort(smem_u32(&empty[st]), (u - 1) & 1, abort)) {
-          *abort = 1;
-          break;
+      int gc = 0;  // chunks issued by this CTA
+      for (int64_t t = blockIdx.x; t < ntiles && !*abort; t += gridDim.x) {
+        int b;
+        uint64_t m0, n0;
+        tm.decode(t, b, m0, n0, BN);
+        const int asl = jd.a.batch_stride ? b : 0, bsl = jd.b.batch_stride ? b : 0;
+        for (int c = 0; c < nchunks; ++c, ++gc) {
+          const int st = gc % NST, u = gc / NST;
+          if (gc >= NST && !mbar_wait_or_abort(smem_u32(&empty[st]), (u - 1) & 1, abort)) {
+            *abort = 1;
+            break;
+          }
+          const uint32_t dst = sbase + st * L::STAGE;
+          const uint32_t bar = smem_u32(&full[st]);
+          mbar_expect_tx(bar, (uint32_t)L::RAW);
+          tma_load_3d(dst, &tmA, bar, c * kBK, (int)m0, asl);
+          tma_load_3d(dst + L::A_BYTES, &tmB, bar, c * kBK, (int)n0, bsl);
         }
-        const uint32_t dst = sbase + st * L::STAGE;
-        const uint32_t bar = smem_u32(&full[st]);
-        mbar_expect_tx(bar, (uint32_t)L::RAW);
-        tma_load_3d(dst, &tmA, bar, c * kBK, (int)m0, asl);
-        tma_load_3d(dst + L::A_BYTES, &tmB, bar, c * kBK, (int)n0, bsl);
-        issued = c + 1;
       }
       if (*abort)  // loads still in flight must land before the CTA may exit
-        for (int c = max(0, issued - NST); c < issued; ++c) mbar_wait_bounded(smem_u32(&full[c % NST]), (c / NST) & 1);
+        for (int c = max(0, gc - NST); c < gc; ++c) mbar_wait_bounded(smem_u32(&full[c % NST]), (c / NST) & 1);
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------------- MMA issuer
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_tf32(kBM, BN);
       bool ok = true;
-      for (int c = 0; c < nchunks && ok; ++c) {
-        const int st = c % NST, u = c / NST;
-        if (!mbar_wait_or_abort(smem_u32(&conv[st]), u & 1, abort)) { ok = false; break; }
-        tc_fence_after();
-        const uint32_t a_hi = sbase + st * L::STAGE, b_hi = a_hi + L::A_BYTES;
-        const uint32_t a_lo = a_hi + L::RAW, b_lo = a_lo + L::A_BYTES;
-        for (int h = 0; h < 2; ++h) {
-          const int w = 2 * c + h;
-          if (w >= nwin) break;
-          const int set = w & 1;
-          if (w >= 2 && !mbar_wait_or_abort(smem_u32(&acce[set]), ((w >> 1) - 1) & 1, abort)) {
-            ok = false;
-            break;
-          }
+      int gc = 0, gw = 0;  // chunks and windows consumed by this CTA
+      for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        for (int c = 0; c < nchunks && ok; ++c, ++gc) {
+          const int st = gc % NST, u = gc / NST;
+          if (!mbar_wait_or_abort(smem_u32(&conv[st]), u & 1, abort)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t d = tmem + (uint32_t)(set * BN);
-          const int t0 = 2 * h, t1 = min(2 * h + 2, ksteps - 4 * c);
-          uint32_t accum = 0;
-          for (int t = t0; t < t1; ++t) {  // corrections while the set is small
-            umma_tf32(d, smem_desc_sw128(a_hi + 32 * t), smem_desc_sw128(b_lo + 32 * t), idesc, accum);
-            accum = 1;
-            umma_tf32(d, smem_desc_sw128(a_lo + 32 * t), smem_desc_sw128(b_hi + 32 * t), idesc, 1u);
+          const uint32_t a_hi = sbase + st * L::STAGE, b_hi = a_hi + L::A_BYTES;
+          const uint32_t a_lo = a_hi + L::RAW, b_lo = a_lo + L::A_BYTES;
+          for (int h = 0; h < 2; ++h) {
+            if (2 * c + h >= nwin) break;
+            const int set = gw & 1;
+            if (gw >= 2 && !mbar_wait_or_abort(smem_u32(&acce[set]), ((gw >> 1) - 1) & 1, abort)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t d = tmem + (uint32_t)(set * BN);
+            const int t0 = 2 * h, t1 = min(2 * h + 2, ksteps - 4 * c);
+            uint32_t accum = 0;
+            for (int k = t0; k < t1; ++k) {  // corrections while the set is small
+              umma_tf32(d, smem_desc_sw128(a_hi + 32 * k), smem_desc_sw128(b_lo + 32 * k), idesc, accum);
+              accum = 1;
+              umma_tf32(d, smem_desc_sw128(a_lo + 32 * k), smem_desc_sw128(b_hi + 32 * k), idesc, 1u);
+            }
+            for (int k = t0; k < t1; ++k)
+              umma_tf32(d, smem_desc_sw128(a_hi + 32 * k), smem_desc_sw128(b_hi + 32 * k), idesc, 1u);
+            umma_commit(smem_u32(&accf[set]));
+            ++gw;
           }
-          for (int t = t0; t < t1; ++t)
-            umma_tf32(d, smem_desc_sw128(a_hi + 32 * t), smem_desc_sw128(b_hi + 32 * t), idesc, 1u);
-          umma_commit(smem_u32(&accf[set]));
+          umma_commit(smem_u32(&empty[st]));
         }
-        umma_commit(smem_u32(&empty[st]));
       }
       if (!ok) *abort = 1;
       // Every MMA of this thread completes before tensor memory is freed.
@@ -192,106 +206,121 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
   } else if (warp >= 4 && warp < 8) {
     // ---------------------------------------------------------------- converters
     const int ct = tid - 128;
-    const float fa = pow2f(sa), fb = pow2f(sb);
-    for (int c = 0; c < nchunks; ++c) {
-      const int st = c % NST, u = c / NST;
-      if (!mbar_wait_or_abort(smem_u32(&full[st]), u & 1, abort)) {
-        *abort = 1;
-        break;
-      }
-      unsigned char* hi = smem + st * L::STAGE;
-      unsigned char* lo = hi + L::RAW;
+    bool ok = true;
+    int gc = 0;
+    for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      int b;
+      uint64_t m0, n0;
+      tm.decode(t, b, m0, n0, BN);
+      const float fa = pow2f(op_shift(jd.a, b)), fb = pow2f(op_shift(jd.b, b));
+      for (int c = 0; c < nchunks; ++c, ++gc) {
+        const int st = gc % NST, u = gc / NST;
+        if (!mbar_wait_or_abort(smem_u32(&full[st]), u & 1, abort)) {
+          *abort = 1;
+          ok = false;
+          break;
+        }
+        unsigned char* hi = smem + st * L::STAGE;
+        unsigned char* lo = hi + L::RAW;
 #pragma unroll 4
-      for (int e = ct; e < L::RAW / 16; e += kConv) {
-        const float4 x = *reinterpret_cast<const float4*>(hi + e * 16);
-        float4 h, l;
-        split4(x, e * 16 < L::A_BYTES ? fa : fb, h, l);
-        *reinterpret_cast<float4*>(hi + e * 16) = h;
-        *reinterpret_cast<float4*>(lo + e * 16) = l;
+        for (int e = ct; e < L::RAW / 16; e += kConv) {
+          const float4 x = *reinterpret_cast<const float4*>(hi + e * 16);
+          float4 h, l;
+          split4(x, e * 16 < L::A_BYTES ? fa : fb, h, l);
+          *reinterpret_cast<float4*>(hi + e * 16) = h;
+          *reinterpret_cast<float4*>(lo + e * 16) = l;
+        }
+        fence_async_smem();
+        mbar_arrive(smem_u32(&conv[st]));
       }
-      fence_async_smem();
-      mbar_arrive(smem_u32(&conv[st]));
     }
   } else if (warp >= 8) {
     // ---------------------------------------------------------------- read-out + epilogue
-    const int q = warp & 3, hf = (warp - 8) >> 2, rt = tid - 256;
+    const int q = warp & 3, hf = (warp - 8) >> 2;
     const int row = 32 * q + lane;
-    const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(hf * HALF);
-    float acc[HALF];
+    const int col0 = hf * HALF;
+    const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)col0;
+    // Row-major float4 stores when the tile's n bits are the output's lowest address bits.
+    const int nbits_tile = jd.nb < (BN == 128 ? 7 : 6) ? jd.nb : (BN == 128 ? 7 : 6);
+    bool rowmajor = nbits_tile >= 2;
+    for (int i = 0; i < nbits_tile; ++i) rowmajor = rowmajor && jd.c_s_n[i] == (1ll << i);
+    const int64_t crow = tCm[row];
+    bool ok = true;
+    int gw = 0;
+    for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      int b;
+      uint64_t m0, n0;
+      tm.decode(t, b, m0, n0, BN);
+      float acc[HALF];
 #pragma unroll
-    for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
-    for (int w = 0; w < nwin; ++w) {
-      const int set = w & 1;
-      if (!mbar_wait_or_abort(smem_u32(&accf[set]), (w >> 1) & 1, abort)) {
-        *abort = 1;
-        break;
-      }
-      tc_fence_after();
-#pragma unroll
-      for (int col = 0; col < HALF; col += 32) {
-        float v0[16], v1[16];
-        tmem_ld16(tl + (uint32_t)(set * BN + col), v0);
-        tmem_ld16(tl + (uint32_t)(set * BN + col + 16), v1);
-        tmem_ld_wait();
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          acc[col + j] += v0[j];
-          acc[col + 16 + j] += v1[j];
+      for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
+      for (int w = 0; w < nwin; ++w, ++gw) {
+        const int set = gw & 1;
+        if (!mbar_wait_or_abort(smem_u32(&accf[set]), (gw >> 1) & 1, abort)) {
+          *abort = 1;
+          ok = false;
+          break;
         }
-      }
-      tc_fence_before();
-      mbar_arrive(smem_u32(&acce[set]));
-    }
-    named_bar(1, kRead);  // every read-out done: all MMAs and loads have finished
-    uint32_t bits = 0;
-    const bool ok = *abort == 0;
-    float* cs = reinterpret_cast<float*>(smem);
-    if (ok) {
+        tc_fence_after();
 #pragma unroll
-      for (int j = 0; j < HALF; j += 4)
-        *reinterpret_cast<float4*>(&cs[row * L::CROW + hf * HALF + j]) =
-            make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
-      if (row < mlim) {
+        for (int col = 0; col < HALF; col += 32) {
+          float v0[16], v1[16];
+          tmem_ld16(tl + (uint32_t)(set * BN + col), v0);
+          tmem_ld16(tl + (uint32_t)(set * BN + col + 16), v1);
+          tmem_ld_wait();
 #pragma unroll
-        for (int j = 0; j < HALF; ++j)
-          if (hf * HALF + j < nlim) bits = max(bits, __float_as_uint(fmaxf(acc[j], 0.f)));
+          for (int j = 0; j < 16; ++j) {
+            acc[col + j] += v0[j];
+            acc[col + 16 + j] += v1[j];
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(smem_u32(&acce[set]));
       }
-    }
-    named_bar(1, kRead);
-    if (ok) {
+      if (!ok) break;
+      const int mlim = (int)min((int64_t)kBM, M - (int64_t)m0);
+      const int nlim = (int)min((int64_t)BN, N - (int64_t)n0);
       float* __restrict__ C = (float*)jd.c_ptr + (int64_t)b * jd.c_batch_stride + deposit(jd.c_s_m, m0) +
                               deposit(jd.c_s_n, n0);
-      // Row-major float4 stores when the tile's n bits are the output's lowest address bits.
-      bool rowmajor = (nlim & 3) == 0;
-      for (int i = 0; (1 << i) < nlim; ++i) rowmajor = rowmajor && jd.c_s_n[i] == (1ll << i);
-      if (rowmajor) {
-        constexpr int V = BN / 4;
-        for (int idx = rt; idx < kBM * V; idx += kRead) {
-          const int r = idx / V, c4 = idx - r * V;
-          if (r < mlim && 4 * c4 < nlim)
-            *reinterpret_cast<float4*>(C + tCm[r] + 4 * c4) = *reinterpret_cast<const float4*>(&cs[r * L::CROW + 4 * c4]);
+      uint32_t bits = 0;
+      if (row < mlim) {
+        if (rowmajor) {
+#pragma unroll
+          for (int j = 0; j < HALF; j += 4)
+            if (col0 + j < nlim)
+              *reinterpret_cast<float4*>(C + crow + col0 + j) = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < HALF; ++j)
+            if (col0 + j < nlim) C[crow + tCn[col0 + j]] = acc[j];
         }
-      } else {
-        for (int idx = rt; idx < kBM * BN; idx += kRead) {
-          const int r = idx & (kBM - 1), c = idx >> 7;
-          if (r < mlim && c < nlim) C[tCm[r] + tCn[c]] = cs[r * L::CROW + c];
-        }
+#pragma unroll
+        for (int j = 0; j < HALF; ++j)
+          if (col0 + j < nlim) bits = max(bits, __float_as_uint(fmaxf(acc[j], 0.f)));
       }
-    }
-    for (int off = 16; off > 0; off >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, off));
-    if (lane == 0) red[warp - 8] = bits;
-    named_bar(1, kRead);
-    if (rt == 0 && ok) {
-      uint32_t m = 0;
-      for (int i = 0; i < kRead / 32; ++i) m = max(m, red[i]);
-      atomicMax(&jd.c_max[b], m);
-      if (tile == 0) jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - sa - sb;
+      for (int off = 16; off > 0; off >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, off));
+      if (lane == 0) atomicMax(&jd.c_max[b], bits);
+      if (m0 == 0 && n0 == 0 && tid == 256)
+        jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - op_shift(jd.a, b) - op_shift(jd.b, b);
     }
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 1) tmem_dealloc(tmem, kCols);
   if (tid == 0 && abort_sh && jd.err) atomicExch(jd.err, 1);
+}
+
+int sm_count() {
+  static int sms[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!sms[dev]) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    sms[dev] = n > 0 ? n : 1;
+  }
+  return sms[dev];
 }
 
 template <int BN, int NST>
@@ -301,13 +330,14 @@ cudaError_t launch_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorM
   cudaError_t e = cudaFuncSetAttribute(k_umma_ws<BN, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::DYN);
   if (e != cudaSuccess) return e;
   constexpr int bn_bits = BN == 128 ? 7 : 6;
+  TileMap tm;
   const int tm_bits = jd.mb > 7 ? jd.mb - 7 : 0;
-  const int tn_bits = jd.nb > bn_bits ? jd.nb - bn_bits : 0;
-  const uint64_t tiles = 1ull << (tm_bits + tn_bits);
-  if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
-  const int gy = nslices < 65535 ? nslices : 65535;
-  const int gz = (nslices + gy - 1) / gy;
-  k_umma_ws<BN, NST><<<dim3((unsigned)tiles, gy, gz), kWsThreads, L::DYN, st>>>(jd, ta, tb, nslices, tn_bits);
+  tm.tn_bits = jd.nb > bn_bits ? jd.nb - bn_bits : 0;
+  tm.tps_bits = tm_bits + tm.tn_bits;
+  if (tm.tps_bits > 40) return cudaErrorInvalidValue;
+  const int64_t ntiles = (int64_t)nslices << tm.tps_bits;
+  const int64_t grid = ntiles < sm_count() ? ntiles : sm_count();
+  k_umma_ws<BN, NST><<<(unsigned)grid, kWsThreads, L::DYN, st>>>(jd, ta, tb, ntiles, tm);
   return cudaGetLastError();
 }
 
