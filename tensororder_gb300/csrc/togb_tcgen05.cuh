@@ -83,10 +83,13 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// Round a finite FP32 value to the nearest TF32 value (10 explicit mantissa
+// bits), ties away from zero, on its IEEE-754 bit pattern: adding half of the
+// dropped 13-bit field to the magnitude bits and clearing the field rounds the
+// magnitude (a carry into the exponent gives the next binade, which is the
+// correctly rounded result).  Two integer operations, full issue rate.
 __device__ __forceinline__ float tf32_rn(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
 // Shared-memory matrix descriptor, K-major, no swizzle: 8-row x 16-byte core

@@ -8,25 +8,31 @@
 //
 // One CTA computes a 128 x BN output tile of one slice with four roles:
 //   warp 0        TMA producer: loads the 32-wide K chunks of A and B (128-byte
-//                 swizzle) into a ring of NST stages;
-//   warps 4-7     converters: split each landed chunk in place into hi and a
-//                 second, identically swizzled lo buffer;
+//                 swizzle) into a ring of NR raw stages;
+//   warps 2-7     converters: split each landed chunk into hi and lo buffers of
+//                 the same swizzled layout in a ring of NC converted stages,
+//                 releasing the raw stage at once, so the loads in flight are
+//                 not held up by the MMAs;
 //   warp 1        MMA issuer: one thread issues the tcgen05.mma of each chunk;
 //   warps 8-15    read-out: drain the tensor-memory accumulators into FP32
 //                 registers and run the epilogue.
 // The tensor core truncates its FP32 accumulation, so one accumulator must not
 // see many large updates.  The K range is therefore cut into windows of 16
 // (two MMA k-steps); each window accumulates into a fresh tensor-memory set
-// (two sets, alternating), correction products first while the set is still
-// small, main products last, and the read-out warps add the window into
-// round-to-nearest registers while the next window's MMAs run.
+// (512 / BN sets used in rotation, so the MMAs run several windows ahead of
+// the read-out), correction products first while the set is still small, main
+// products last, and the read-out warps add the window into round-to-nearest
+// registers while later windows' MMAs run.
 //
 // The kernel is persistent (one CTA per SM walking the tiles), so the next
 // tile's loads, conversions and first MMAs overlap the current tile's
-// epilogue.  Each read-out thread owns one output row: it stores its columns
-// straight from registers (float4 stores when the output's lowest address bits
-// are the tile's n bits), then the slice maximum and exponent are recorded
-// like in the other split-form kernels.
+// epilogue.  Each read-out thread owns one output row.  When the tile's n bits
+// are the output's lowest address bits, every read-out warp transposes its 32
+// rows through a private shared-memory area so that each store instruction
+// writes whole 128-byte row segments; otherwise lanes store their rows'
+// columns directly (consecutive rows, coalesced when the m bits are lowest).
+// The slice maximum and exponent are recorded like in the other split-form
+// kernels.
 //
 // Operands that do not vary with the slice (slice-invariant intermediates) use
 // a tensor map with one slice and slice coordinate 0.  Every wait is bounded:
@@ -45,14 +51,15 @@ namespace {
 
 constexpr int kWsThreads = 512;  // 16 warps
 
-template <int BN, int NST>
+template <int BN, int NR, int NC>
 struct WsSmem {
   static constexpr int A_BYTES = kBM * kBK * 4;
   static constexpr int B_BYTES = BN * kBK * 4;
-  static constexpr int RAW = A_BYTES + B_BYTES;  // TMA target, converted in place to hi
-  static constexpr int STAGE = 2 * RAW;          // [hi: A | B][lo: A | B]
-  static constexpr int DYN = NST * STAGE + 1024;
-  static_assert(DYN <= 227 * 1024, "shared memory budget");
+  static constexpr int RAW = A_BYTES + B_BYTES;  // TMA target: [A | B]
+  static constexpr int CONV = 2 * RAW;           // [hi: A | B][lo: A | B]
+  static constexpr int STG = 8 * 32 * 32 * 4;   // per read-out warp: 32 rows x 32 columns of staging
+  static constexpr int DYN = NR * RAW + NC * CONV + STG + 1024;
+  static_assert(DYN + 1536 <= 227 * 1024, "shared memory budget");
 };
 
 __device__ __forceinline__ void split4(float4 x, float f, float4& hi, float4& lo) {
@@ -83,21 +90,22 @@ struct TileMap {
 // The stage ring and the two accumulator sets run continuously across tiles,
 // so the next tile's loads, conversions and first MMAs overlap the current
 // tile's epilogue.
-template <int BN, int NST>
+template <int BN, int NR, int NC>
 __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant__ JoinDesc jd,
                                                           const __grid_constant__ CUtensorMap tmA,
                                                           const __grid_constant__ CUtensorMap tmB,
                                                           int64_t ntiles, TileMap tm) {
-  using L = WsSmem<BN, NST>;
-  constexpr int HALF = BN / 2;        // columns per read-out warp
-  constexpr uint32_t kCols = 2 * BN;  // two accumulator sets
-  constexpr int kConv = 128;          // converter threads
+  using L = WsSmem<BN, NR, NC>;
+  constexpr int HALF = BN / 2;         // columns per read-out warp
+  constexpr uint32_t kCols = 512;      // all of tensor memory (one CTA per SM)
+  constexpr int NSETS = kCols / BN;    // accumulator sets in rotation
+  constexpr int kConv = 192;          // converter threads (warps 2-7)
   constexpr int kRead = 256;          // read-out threads
   extern __shared__ unsigned char dyn_raw[];
-  __shared__ __align__(8) uint64_t full[NST], conv[NST], empty[NST], accf[2], acce[2], fin;
+  __shared__ __align__(8) uint64_t full[NR], rawfree[NR], conv[NC], cfree[NC], accf[NSETS], acce[NSETS], fin;
   __shared__ uint32_t tmem_sh;
   __shared__ int abort_sh;
-  __shared__ int64_t tCm[kBM], tCn[BN];
+  __shared__ int32_t tCm[kBM], tCn[BN];  // output offsets within a tile (< 2^31 per slice)
 
   // After one CTA's wait expired the result is void: later CTAs leave at once.
   if (jd.err && *(volatile int32_t*)jd.err) return;
@@ -109,15 +117,18 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
   const int nwin = (ksteps + 1) / 2;              // windows of two k-steps
   const int nchunks = (nwin + 1) / 2;             // TMA chunks of four k-steps
 
-  for (int i = tid; i < kBM; i += kWsThreads) tCm[i] = deposit(jd.c_s_m, i);
-  for (int i = tid; i < BN; i += kWsThreads) tCn[i] = deposit(jd.c_s_n, i);
+  for (int i = tid; i < kBM; i += kWsThreads) tCm[i] = (int32_t)deposit(jd.c_s_m, i);
+  for (int i = tid; i < BN; i += kWsThreads) tCn[i] = (int32_t)deposit(jd.c_s_n, i);
   if (tid == 0) {
-    for (int i = 0; i < NST; ++i) {
+    for (int i = 0; i < NR; ++i) {
       mbar_init(smem_u32(&full[i]), 1);
-      mbar_init(smem_u32(&conv[i]), kConv);
-      mbar_init(smem_u32(&empty[i]), 1);
+      mbar_init(smem_u32(&rawfree[i]), kConv);
     }
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < NC; ++i) {
+      mbar_init(smem_u32(&conv[i]), kConv);
+      mbar_init(smem_u32(&cfree[i]), 1);
+    }
+    for (int i = 0; i < NSETS; ++i) {
       mbar_init(smem_u32(&accf[i]), 1);
       mbar_init(smem_u32(&acce[i]), kRead);
     }
@@ -145,12 +156,12 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
         tm.decode(t, b, m0, n0, BN);
         const int asl = jd.a.batch_stride ? b : 0, bsl = jd.b.batch_stride ? b : 0;
         for (int c = 0; c < nchunks; ++c, ++gc) {
-          const int st = gc % NST, u = gc / NST;
-          if (gc >= NST && !mbar_wait_or_abort(smem_u32(&empty[st]), (u - 1) & 1, abort)) {
+          const int st = gc % NR, u = gc / NR;
+          if (gc >= NR && !mbar_wait_or_abort(smem_u32(&rawfree[st]), (u - 1) & 1, abort)) {
             *abort = 1;
             break;
           }
-          const uint32_t dst = sbase + st * L::STAGE;
+          const uint32_t dst = sbase + st * L::RAW;
           const uint32_t bar = smem_u32(&full[st]);
           mbar_expect_tx(bar, (uint32_t)L::RAW);
           tma_load_3d(dst, &tmA, bar, c * kBK, (int)m0, asl);
@@ -158,7 +169,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
         }
       }
       if (*abort)  // loads still in flight must land before the CTA may exit
-        for (int c = max(0, gc - NST); c < gc; ++c) mbar_wait_bounded(smem_u32(&full[c % NST]), (c / NST) & 1);
+        for (int c = max(0, gc - NR); c < gc; ++c) mbar_wait_bounded(smem_u32(&full[c % NR]), (c / NR) & 1);
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------------- MMA issuer
@@ -168,15 +179,15 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
       int gc = 0, gw = 0;  // chunks and windows consumed by this CTA
       for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
         for (int c = 0; c < nchunks && ok; ++c, ++gc) {
-          const int st = gc % NST, u = gc / NST;
+          const int st = gc % NC, u = gc / NC;
           if (!mbar_wait_or_abort(smem_u32(&conv[st]), u & 1, abort)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t a_hi = sbase + st * L::STAGE, b_hi = a_hi + L::A_BYTES;
+          const uint32_t a_hi = sbase + NR * L::RAW + st * L::CONV, b_hi = a_hi + L::A_BYTES;
           const uint32_t a_lo = a_hi + L::RAW, b_lo = a_lo + L::A_BYTES;
           for (int h = 0; h < 2; ++h) {
             if (2 * c + h >= nwin) break;
-            const int set = gw & 1;
-            if (gw >= 2 && !mbar_wait_or_abort(smem_u32(&acce[set]), ((gw >> 1) - 1) & 1, abort)) {
+            const int set = gw % NSETS;
+            if (gw >= NSETS && !mbar_wait_or_abort(smem_u32(&acce[set]), (gw / NSETS - 1) & 1, abort)) {
               ok = false;
               break;
             }
@@ -194,7 +205,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
             umma_commit(smem_u32(&accf[set]));
             ++gw;
           }
-          umma_commit(smem_u32(&empty[st]));
+          umma_commit(smem_u32(&cfree[st]));
         }
       }
       if (!ok) *abort = 1;
@@ -203,9 +214,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
       mbar_wait_bounded(smem_u32(&fin), 0);
     }
     __syncwarp();
-  } else if (warp >= 4 && warp < 8) {
+  } else if (warp >= 2 && warp < 8) {
     // ---------------------------------------------------------------- converters
-    const int ct = tid - 128;
+    const int ct = tid - 64;
     bool ok = true;
     int gc = 0;
     for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
@@ -214,29 +225,32 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
       tm.decode(t, b, m0, n0, BN);
       const float fa = pow2f(op_shift(jd.a, b)), fb = pow2f(op_shift(jd.b, b));
       for (int c = 0; c < nchunks; ++c, ++gc) {
-        const int st = gc % NST, u = gc / NST;
-        if (!mbar_wait_or_abort(smem_u32(&full[st]), u & 1, abort)) {
+        const int rs = gc % NR, ru = gc / NR, cs = gc % NC, cu = gc / NC;
+        if (!mbar_wait_or_abort(smem_u32(&full[rs]), ru & 1, abort) ||
+            (gc >= NC && !mbar_wait_or_abort(smem_u32(&cfree[cs]), (cu - 1) & 1, abort))) {
           *abort = 1;
           ok = false;
           break;
         }
-        unsigned char* hi = smem + st * L::STAGE;
+        const unsigned char* raw = smem + rs * L::RAW;
+        unsigned char* hi = smem + NR * L::RAW + cs * L::CONV;
         unsigned char* lo = hi + L::RAW;
 #pragma unroll 4
         for (int e = ct; e < L::RAW / 16; e += kConv) {
-          const float4 x = *reinterpret_cast<const float4*>(hi + e * 16);
+          const float4 x = *reinterpret_cast<const float4*>(raw + e * 16);
           float4 h, l;
           split4(x, e * 16 < L::A_BYTES ? fa : fb, h, l);
           *reinterpret_cast<float4*>(hi + e * 16) = h;
           *reinterpret_cast<float4*>(lo + e * 16) = l;
         }
+        mbar_arrive(smem_u32(&rawfree[rs]));  // raw stage read: the next load may land there
         fence_async_smem();
-        mbar_arrive(smem_u32(&conv[st]));
+        mbar_arrive(smem_u32(&conv[cs]));
       }
     }
   } else if (warp >= 8) {
     // ---------------------------------------------------------------- read-out + epilogue
-    const int q = warp & 3, hf = (warp - 8) >> 2;
+    const int q = warp & 3, hf = (warp - 8) >> 2, rt = tid - 256;
     const int row = 32 * q + lane;
     const int col0 = hf * HALF;
     const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)col0;
@@ -244,10 +258,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
     const int nbits_tile = jd.nb < (BN == 128 ? 7 : 6) ? jd.nb : (BN == 128 ? 7 : 6);
     bool rowmajor = nbits_tile >= 2;
     for (int i = 0; i < nbits_tile; ++i) rowmajor = rowmajor && jd.c_s_n[i] == (1ll << i);
-    const int64_t crow = tCm[row];
-    bool ok = true;
+    float4* wst = reinterpret_cast<float4*>(smem + NR * L::RAW + NC * L::CONV) + (warp - 8) * 256;  // 32 rows x 8 float4
     int gw = 0;
-    for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
       int b;
       uint64_t m0, n0;
       tm.decode(t, b, m0, n0, BN);
@@ -255,10 +268,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
 #pragma unroll
       for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
       for (int w = 0; w < nwin; ++w, ++gw) {
-        const int set = gw & 1;
-        if (!mbar_wait_or_abort(smem_u32(&accf[set]), (gw >> 1) & 1, abort)) {
+        const int set = gw % NSETS;
+        if (!mbar_wait_or_abort(smem_u32(&accf[set]), (gw / NSETS) & 1, abort)) {
           *abort = 1;
-          ok = false;
           break;
         }
         tc_fence_after();
@@ -277,30 +289,45 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
         tc_fence_before();
         mbar_arrive(smem_u32(&acce[set]));
       }
-      if (!ok) break;
+      if (*abort) break;
       const int mlim = (int)min((int64_t)kBM, M - (int64_t)m0);
       const int nlim = (int)min((int64_t)BN, N - (int64_t)n0);
       float* __restrict__ C = (float*)jd.c_ptr + (int64_t)b * jd.c_batch_stride + deposit(jd.c_s_m, m0) +
                               deposit(jd.c_s_n, n0);
       uint32_t bits = 0;
       if (row < mlim) {
-        if (rowmajor) {
-#pragma unroll
-          for (int j = 0; j < HALF; j += 4)
-            if (col0 + j < nlim)
-              *reinterpret_cast<float4*>(C + crow + col0 + j) = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
-        } else {
-#pragma unroll
-          for (int j = 0; j < HALF; ++j)
-            if (col0 + j < nlim) C[crow + tCn[col0 + j]] = acc[j];
-        }
 #pragma unroll
         for (int j = 0; j < HALF; ++j)
           if (col0 + j < nlim) bits = max(bits, __float_as_uint(fmaxf(acc[j], 0.f)));
       }
+      if (rowmajor) {
+        // 32 columns at a time through this warp's staging area: each lane
+        // writes its row's eight float4, then one store instruction covers four
+        // full 128-byte row segments (float4 slots XOR-swizzled by the row).
+#pragma unroll
+        for (int p = 0; p < HALF; p += 32) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            wst[lane * 8 + (j ^ (lane & 7))] =
+                make_float4(acc[p + 4 * j], acc[p + 4 * j + 1], acc[p + 4 * j + 2], acc[p + 4 * j + 3]);
+          __syncwarp();
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const int r = (lane >> 3) + 4 * k, c = lane & 7, gr = 32 * q + r;
+            if (gr < mlim && col0 + p + 4 * c < nlim)
+              *reinterpret_cast<float4*>(C + tCm[gr] + col0 + p + 4 * c) = wst[r * 8 + (c ^ (r & 7))];
+          }
+          __syncwarp();
+        }
+      } else if (row < mlim) {
+        const int64_t crow = tCm[row];
+#pragma unroll
+        for (int j = 0; j < HALF; ++j)
+          if (col0 + j < nlim) C[crow + tCn[col0 + j]] = acc[j];
+      }
       for (int off = 16; off > 0; off >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, off));
-      if (lane == 0) atomicMax(&jd.c_max[b], bits);
-      if (m0 == 0 && n0 == 0 && tid == 256)
+      if (lane == 0 && bits) atomicMax(&jd.c_max[b], bits);
+      if (m0 == 0 && n0 == 0 && rt == 0)
         jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - op_shift(jd.a, b) - op_shift(jd.b, b);
     }
   }
@@ -323,11 +350,11 @@ int sm_count() {
   return sms[dev];
 }
 
-template <int BN, int NST>
+template <int BN, int NR, int NC>
 cudaError_t launch_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorMap& tb, int nslices,
                       cudaStream_t st) {
-  using L = WsSmem<BN, NST>;
-  cudaError_t e = cudaFuncSetAttribute(k_umma_ws<BN, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::DYN);
+  using L = WsSmem<BN, NR, NC>;
+  cudaError_t e = cudaFuncSetAttribute(k_umma_ws<BN, NR, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::DYN);
   if (e != cudaSuccess) return e;
   constexpr int bn_bits = BN == 128 ? 7 : 6;
   TileMap tm;
@@ -337,7 +364,7 @@ cudaError_t launch_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorM
   if (tm.tps_bits > 40) return cudaErrorInvalidValue;
   const int64_t ntiles = (int64_t)nslices << tm.tps_bits;
   const int64_t grid = ntiles < sm_count() ? ntiles : sm_count();
-  k_umma_ws<BN, NST><<<(unsigned)grid, kWsThreads, L::DYN, st>>>(jd, ta, tb, ntiles, tm);
+  k_umma_ws<BN, NR, NC><<<(unsigned)grid, kWsThreads, L::DYN, st>>>(jd, ta, tb, ntiles, tm);
   return cudaGetLastError();
 }
 
@@ -347,8 +374,8 @@ int umma_ws_box_rows_b(int nb) { return nb >= 7 ? 128 : 64; }
 
 cudaError_t launch_umma_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorMap& tb, int nslices,
                            cudaStream_t st) {
-  if (jd.nb >= 7) return launch_ws<128, 3>(jd, ta, tb, nslices, st);
-  return launch_ws<64, 4>(jd, ta, tb, nslices, st);
+  if (jd.nb >= 7) return launch_ws<128, 2, 2>(jd, ta, tb, nslices, st);
+  return launch_ws<64, 4, 2>(jd, ta, tb, nslices, st);
 }
 
 }  // namespace togb
