@@ -205,6 +205,12 @@ class DeviceProgram:
         check(lib().togb_program_result(self._h, _stream_handle(stream), out.ctypes.data_as(_f64p), None, n))
         return out.reshape((2,) * int(self.info.root_rank))
 
+    def partial(self, stream=None):
+        """This program's accumulated result as a sharding partial: the
+        compensated sum (rounded once) and a zero compensation."""
+        out = self.result(stream).reshape(-1)
+        return out, np.zeros_like(out)
+
     def set_timing(self, enable=True):
         check(lib().togb_program_set_timing(self._h, 1 if enable else 0))
 
