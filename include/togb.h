@@ -114,6 +114,19 @@ togb_status togb_program_result(togb_program* prog, void* stream, double* out, d
  * for every slice or 0 when it runs once per call.  n = num_joins. */
 togb_status togb_program_joins(const togb_program* prog, int mode, int32_t* out, int32_t n);
 
+/* Choose the kernel of join `join` in `mode` (kernel ids as in
+ * togb_program_joins; -1 restores the default).  A kernel that cannot run the
+ * join in that form -- the split form's leaf residuals are applied only by the
+ * thread-per-output and reduction kernels, the tensor-core kernel needs
+ * M, N >= 64 and K >= 4 -- is rejected with TOGB_ERR_UNSUPPORTED.  The count
+ * does not depend on the choice beyond the form's tolerance; only the speed
+ * does.  No counterpart in the reference (numpy_apis.py:42-43 always calls
+ * np.tensordot). */
+togb_status togb_program_set_kernel(togb_program* prog, int mode, int32_t join, int32_t kernel);
+/* *allowed = 1 when togb_program_set_kernel would accept the choice. */
+togb_status togb_program_kernel_allowed(const togb_program* prog, int mode, int32_t join, int32_t kernel,
+                                        int32_t* allowed);
+
 /* Per-join device time of the last run with togb_program_set_timing(prog, 1):
  * `ms[j]` for each join in post-order (n = num_joins). */
 togb_status togb_program_set_timing(togb_program* prog, int enable);
@@ -154,6 +167,26 @@ togb_status togb_probe_peak(int kind, void* stream, double* flops_per_second);
  * work overlaps on the GPU race, so serialise them.  Queued on `stream`. */
 togb_status togb_contract_static_f64(const togb_program_desc* desc, const double* d_leaf_values,
                                      double* d_out, void* stream);
+
+/* The learned cost model's network: an MLP F -> H -> H -> 1 (ReLU hidden
+ * layers, FP32) on the device.  No counterpart in the reference, whose only
+ * cost model is the FLOP/memory estimate of contraction_tree.pyx:382-496.
+ * `params` holds togb_mlp_param_count(F, H) floats laid out
+ * W1[F][H] b1[H] W2[H][H] b2[H] W3[H] b3; `scratch` holds
+ * togb_mlp_scratch_floats(B, H) floats.  All pointers are device memory;
+ * every call is queued on `stream`. */
+int64_t togb_mlp_param_count(int F, int H);
+int64_t togb_mlp_scratch_floats(int B, int H);
+/* y[B] = network(x[B][F]). */
+togb_status togb_mlp_forward(const float* params, int F, int H, const float* x, int B, float* y, float* scratch,
+                             void* stream);
+/* grads (same layout as params) of the mean squared error against target[B];
+ * *loss (device, may be NULL) receives that error. */
+togb_status togb_mlp_loss_grad(const float* params, int F, int H, const float* x, const float* target, int B,
+                               float* grads, float* loss, float* scratch, void* stream);
+/* One Adam step (bias-corrected, step >= 1) over n parameters. */
+togb_status togb_mlp_adam(float* params, const float* grads, float* m, float* v, int64_t n, float lr, float beta1,
+                          float beta2, float eps, int32_t step, void* stream);
 
 const char* togb_last_error(void);
 int togb_version(void);

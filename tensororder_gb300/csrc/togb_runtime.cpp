@@ -62,6 +62,7 @@ struct Node {
   std::vector<int> m_lsb, n_lsb, k_lsb;     // GEMM bit order, least significant first
   int64_t off = -1;              // arena offset (elements), joins only
   int kernel = togb::K_DIRECT;
+  int kernel_set[2] = {-1, -1}; // per-form kernel chosen by the caller (togb_program_set_kernel), -1 = default
   bool dep = true;               // depends on the slice (reads a sliced leaf, directly or below)
   int slot = -1;                 // joins: index among the joins of its phase (metadata row)
 };
@@ -447,10 +448,34 @@ void fill_operand(const togb_program* p, const Node& X, const std::vector<int>& 
 // Kernel for a join in the split form: GEMM-sized joins of two intermediates
 // go to the tensor cores; leaf operands need their FP32 residual, which only
 // the CUDA-core kernels apply.
-int split_kernel(const togb_program* p, const Node& J) {
+int default_split_kernel(const togb_program* p, const Node& J) {
   const bool leaf = p->nodes[J.left].leaf >= 0 || p->nodes[J.right].leaf >= 0;
   if (J.kernel == togb::K_TILED) return leaf ? togb::K_DIRECT : togb::K_UMMA;
   return J.kernel;
+}
+
+// Kernel of a join in a form: the caller's choice if set, else the default.
+int join_kernel(const togb_program* p, const Node& J, int mode) {
+  const int m = mode == TOGB_MODE_SPLIT ? 1 : 0;
+  if (J.kernel_set[m] >= 0) return J.kernel_set[m];
+  return m ? default_split_kernel(p, J) : J.kernel;
+}
+
+int split_kernel(const togb_program* p, const Node& J) { return join_kernel(p, J, TOGB_MODE_SPLIT); }
+
+// Kernels a join may run in a form.  Every kernel reads any layout; the
+// limits are numerical (the split form's leaf residuals are applied only by
+// the thread-per-output and reduction kernels) and launch-size limits.
+bool kernel_allowed(const togb_program* p, const Node& J, int mode, int kernel) {
+  const int mb = (int)J.m_lsb.size(), nb = (int)J.n_lsb.size(), kb = (int)J.k_lsb.size();
+  const bool leaf = p->nodes[J.left].leaf >= 0 || p->nodes[J.right].leaf >= 0;
+  switch (kernel) {
+    case togb::K_DIRECT: return true;
+    case togb::K_REDUCE: return mb + nb <= 20;  // one CTA per output entry and slice
+    case togb::K_TILED: return mode == TOGB_MODE_F64 || !leaf;
+    case togb::K_UMMA: return mode == TOGB_MODE_SPLIT && !leaf && mb >= 6 && nb >= 6 && kb >= 2;
+    default: return false;
+  }
 }
 
 // A split-form intermediate operand stored as a row-major [rows][K] matrix,
@@ -585,7 +610,7 @@ togb_status enqueue_phase(togb_program* p, int mode, bool once, int nb, cudaStre
     const int j = js[i];
     if (ev) TOGB_CUDA(cudaEventRecord((*ev)[i], st));
     const Node& J = p->nodes[p->joins[j]];
-    const int kernel = mode == TOGB_MODE_SPLIT ? split_kernel(p, J) : J.kernel;
+    const int kernel = join_kernel(p, J, mode);
     cudaError_t e;
     if (kernel == togb::K_UMMA && mode == TOGB_MODE_SPLIT && p->use_tma[j])
       e = togb::launch_umma(p->jds[j], &p->tmaps[2 * j], &p->tmaps[2 * j + 1], p->d_s0, launch_slices, st);
@@ -837,9 +862,35 @@ togb_status togb_program_joins(const togb_program* p, int mode, int32_t* out, in
     out[5 * j + 0] = (int32_t)J.m_lsb.size();
     out[5 * j + 1] = (int32_t)J.n_lsb.size();
     out[5 * j + 2] = (int32_t)J.k_lsb.size();
-    out[5 * j + 3] = mode == TOGB_MODE_SPLIT ? split_kernel(p, J) : J.kernel;
+    out[5 * j + 3] = join_kernel(p, J, mode);
     out[5 * j + 4] = J.dep ? 1 : 0;
   }
+  return TOGB_OK;
+}
+
+togb_status togb_program_set_kernel(togb_program* p, int mode, int32_t join, int32_t kernel) {
+  if (!p) return fail(TOGB_ERR_INVALID, "null program");
+  if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
+  if (join < 0 || join >= (int32_t)p->joins.size()) return fail(TOGB_ERR_INVALID, "join index out of range");
+  Node& J = p->nodes[p->joins[join]];
+  if (kernel >= 0 && !kernel_allowed(p, J, mode, kernel))
+    return fail(TOGB_ERR_UNSUPPORTED, "kernel " + std::to_string(kernel) + " cannot run join " + std::to_string(join));
+  const int m = mode == TOGB_MODE_SPLIT ? 1 : 0;
+  if (J.kernel_set[m] != kernel) {
+    J.kernel_set[m] = kernel < 0 ? -1 : kernel;
+    if (p->cur_mode == mode) {  // descriptors (TMA maps, operand order) follow the kernel choice
+      clear_graphs(p);
+      p->cur_mode = -1;
+    }
+  }
+  return TOGB_OK;
+}
+
+togb_status togb_program_kernel_allowed(const togb_program* p, int mode, int32_t join, int32_t kernel,
+                                        int32_t* allowed) {
+  if (!p || !allowed) return fail(TOGB_ERR_INVALID, "null argument");
+  if (join < 0 || join >= (int32_t)p->joins.size()) return fail(TOGB_ERR_INVALID, "join index out of range");
+  *allowed = kernel_allowed(p, p->nodes[p->joins[join]], mode, kernel) ? 1 : 0;
   return TOGB_OK;
 }
 

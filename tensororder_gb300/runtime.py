@@ -73,7 +73,7 @@ EXPORTS = [
     "togb_version", "togb_last_error", "togb_program_create", "togb_program_info_get",
     "togb_program_reset", "togb_program_run", "togb_program_result", "togb_program_set_timing",
     "togb_program_join_times", "togb_program_destroy", "togb_tensordot_f64", "togb_probe_peak",
-    "togb_contract_static_f64", "togb_program_joins",
+    "togb_contract_static_f64", "togb_program_joins", "togb_program_set_kernel", "togb_program_kernel_allowed",
 ]
 
 KERNEL_NAMES = {0: "direct", 1: "tiled", 2: "reduce", 3: "tensor"}
@@ -111,6 +111,8 @@ def lib():
     L.togb_probe_peak.argtypes = [ctypes.c_int, c_void, ctypes.POINTER(ctypes.c_double)]
     L.togb_contract_static_f64.argtypes = [ctypes.POINTER(ProgramDesc), c_void, c_void, c_void]
     L.togb_program_joins.argtypes = [c_void, ctypes.c_int, _i32p, ctypes.c_int32]
+    L.togb_program_set_kernel.argtypes = [c_void, ctypes.c_int, ctypes.c_int32, ctypes.c_int32]
+    L.togb_program_kernel_allowed.argtypes = [c_void, ctypes.c_int, ctypes.c_int32, ctypes.c_int32, _i32p]
     for name in EXPORTS:
         if name not in ("togb_version", "togb_last_error", "togb_program_destroy"):
             getattr(L, name).restype = ctypes.c_int
@@ -228,6 +230,19 @@ class DeviceProgram:
         out = np.zeros((max(n, 1), 5), dtype=np.int32)
         check(lib().togb_program_joins(self._h, int(mode), out.ctypes.data_as(_i32p), n))
         return out[:n]
+
+    def set_kernel(self, mode, join, kernel):
+        """Run ``join`` with ``kernel`` (an id of ``KERNEL_NAMES``; -1 = default) in ``mode``."""
+        check(lib().togb_program_set_kernel(self._h, int(mode), int(join), int(kernel)))
+
+    def kernel_allowed(self, mode, join, kernel):
+        out = ctypes.c_int32()
+        check(lib().togb_program_kernel_allowed(self._h, int(mode), int(join), int(kernel), ctypes.byref(out)))
+        return bool(out.value)
+
+    def allowed_kernels(self, mode):
+        """Per join, the kernel ids it may run in ``mode``."""
+        return [[k for k in KERNEL_NAMES if self.kernel_allowed(mode, j, k)] for j in range(int(self.info.num_joins))]
 
     def close(self):
         if getattr(self, "_h", None):
