@@ -168,6 +168,23 @@ togb_status togb_probe_peak(int kind, void* stream, double* flops_per_second);
 togb_status togb_contract_static_f64(const togb_program_desc* desc, const double* d_leaf_values,
                                      double* d_out, void* stream);
 
+/* A batch of programs (instances of uneven size, each with its own plan,
+ * slice count and workspace) contracted by one CUDA graph: every program's
+ * complete count -- accumulator reset, slice-invariant joins, all chunks of
+ * slices -- runs on internal stream i % nstreams, forked from and joined back
+ * into the caller's stream.  The programs' kernels (togb_program_set_kernel)
+ * and workspaces are fixed when the batch is created; a program may belong
+ * to one live batch at a time and must not be run on its own meanwhile.  The
+ * reference contracts instances one after another (execution.py:122-152). */
+typedef struct togb_batch togb_batch;
+togb_status togb_batch_create(togb_program* const* progs, int32_t n, int mode, void* const* workspaces,
+                              const size_t* workspace_bytes, int32_t nstreams, togb_batch** out);
+/* One step: every program's count, queued on `stream`. */
+togb_status togb_batch_run(togb_batch* batch, void* stream);
+/* Wait for `stream`; out[i] = count of program i (scalar roots only). */
+togb_status togb_batch_results(togb_batch* batch, void* stream, double* out, int32_t n);
+void togb_batch_destroy(togb_batch* batch);
+
 /* The learned cost model's network: an MLP F -> H -> H -> 1 (ReLU hidden
  * layers, FP32) on the device.  No counterpart in the reference, whose only
  * cost model is the FLOP/memory estimate of contraction_tree.pyx:382-496.

@@ -68,19 +68,27 @@ __device__ __forceinline__ T dot_k(const JoinDesc& jd, const T* __restrict__ A, 
   } else {
     int64_t ka = 0, kb = 0;
     if (MODE == 1) {
+      // FP32 partials of 16 terms, added into a compensated (Neumaier) sum:
+      // the error stays near 16 rounding errors whatever K is.
       const float* alo = jd.a.ptr_lo ? (const float*)jd.a.ptr_lo + oa : nullptr;
       const float* blo = jd.b.ptr_lo ? (const float*)jd.b.ptr_lo + ob : nullptr;
-      float f = 0.f;
-      for (int k = 0; k < K; ++k) {
-        const float av = (float)A[oa + ka] * fa, bv = (float)B[ob + kb] * fb;
-        if (alo) f = fmaf(alo[ka] * fa, bv, f);
-        if (blo) f = fmaf(av, blo[kb] * fb, f);
-        f = fmaf(av, bv, f);
-        const int t = __ffs(~k) - 1;
-        ka += jd.a.dk[t];
-        kb += jd.b.dk[t];
+      float sum = 0.f, comp = 0.f;
+      for (int k0 = 0; k0 < K; k0 += 16) {
+        float f = 0.f;
+        for (int k = k0; k < k0 + 16 && k < K; ++k) {
+          const float av = (float)A[oa + ka] * fa, bv = (float)B[ob + kb] * fb;
+          if (alo) f = fmaf(alo[ka] * fa, bv, f);
+          if (blo) f = fmaf(av, blo[kb] * fb, f);
+          f = fmaf(av, bv, f);
+          const int t = __ffs(~k) - 1;
+          ka += jd.a.dk[t];
+          kb += jd.b.dk[t];
+        }
+        const float t = sum + f;
+        comp += fabsf(sum) >= fabsf(f) ? (sum - t) + f : (f - t) + sum;
+        sum = t;
       }
-      return (T)f;
+      return (T)(sum + comp);
     } else {
       T acc = 0;
       for (int k = 0; k < K; ++k) {
@@ -244,11 +252,14 @@ __global__ void __launch_bounds__(kThreads) k_tiled(const __grid_constant__ Join
   __syncthreads();
 
   const int tx = tid & 15, ty = tid >> 4;
-  T acc[4][4];
+  // Split form: each 16-wide K chunk accumulates into fresh FP32 partials,
+  // which are added into a compensated (Neumaier) running sum, so the error
+  // does not grow with K.
+  T acc[4][4], comp[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0;
+    for (int j = 0; j < 4; ++j) acc[i][j] = comp[i][j] = 0;
 
   for (int64_t k0 = 0; k0 < K; k0 += BK) {
     const int64_t dak = deposit(jd.a.s_k, (uint64_t)k0);
@@ -274,17 +285,49 @@ __global__ void __launch_bounds__(kThreads) k_tiled(const __grid_constant__ Join
       Bs[kk][i] = v;
     }
     __syncthreads();
+    if constexpr (MODE == 0) {
 #pragma unroll
-    for (int kk = 0; kk < BK; ++kk) {
-      T av[4], bv[4];
-      load4(&As[kk][ty * 4], av);
-      load4(&Bs[kk][tx * 4], bv);
+      for (int kk = 0; kk < BK; ++kk) {
+        T av[4], bv[4];
+        load4(&As[kk][ty * 4], av);
+        load4(&Bs[kk][tx * 4], bv);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+      }
+    } else {
+      T part[4][4];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+        for (int j = 0; j < 4; ++j) part[i][j] = 0;
+#pragma unroll
+      for (int kk = 0; kk < BK; ++kk) {
+        T av[4], bv[4];
+        load4(&As[kk][ty * 4], av);
+        load4(&Bs[kk][tx * 4], bv);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) part[i][j] = fma(av[i], bv[j], part[i][j]);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const T t = acc[i][j] + part[i][j];
+          comp[i][j] += fabs(acc[i][j]) >= fabs(part[i][j]) ? (acc[i][j] - t) + part[i][j] : (part[i][j] - t) + acc[i][j];
+          acc[i][j] = t;
+        }
     }
     __syncthreads();
+  }
+  if (MODE == 1) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] += comp[i][j];
   }
 
   T* __restrict__ C = (T*)jd.c_ptr + (int64_t)b * jd.c_batch_stride + deposit(jd.c_s_m, m0) +

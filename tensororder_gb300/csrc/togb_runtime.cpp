@@ -995,6 +995,155 @@ void togb_program_destroy(togb_program* p) {
   delete p;
 }
 
+// ---------------------------------------------------------------------------
+// Batches: many programs (instances of uneven size, each with its own plan and
+// slice count) contracted by one CUDA graph.  Program i runs on internal
+// stream i % nstreams, so independent instances overlap on the GPU; the graph
+// forks from the caller's stream and joins back into it.
+struct togb_batch {
+  std::vector<togb_program*> progs;
+  std::vector<char*> ws;
+  std::vector<int64_t> B;
+  int mode = 0;
+  std::vector<cudaStream_t> streams;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaStream_t cap = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+void batch_free(togb_batch* b) {
+  if (!b) return;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (auto s : b->streams) cudaStreamDestroy(s);
+  for (auto e : b->joins) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->cap) cudaStreamDestroy(b->cap);
+  delete b;
+}
+
+// All of program p's work for one count, queued on st: accumulator reset,
+// slice-invariant joins, then every chunk of slices.
+togb_status enqueue_count(togb_program* p, int mode, int64_t B, cudaStream_t st) {
+  const int64_t E = pow2(p->nodes[p->root].rank);
+  TOGB_CUDA(cudaMemsetAsync(p->d_acc, 0, 2 * E * 8, st));
+  togb_status r = enqueue_phase(p, mode, true, 1, st, nullptr);
+  for (int64_t s = 0; r == TOGB_OK && s < p->num_slices; s += B) {
+    const int nb = (int)std::min<int64_t>(B, p->num_slices - s);
+    cudaError_t e = togb::launch_set_s0(p->d_s0, s, st);
+    if (e != cudaSuccess) return cuda_fail(e, "slice base update");
+    r = enqueue_phase(p, mode, false, nb, st, nullptr);
+  }
+  return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+togb_status togb_batch_create(togb_program* const* progs, int32_t n, int mode, void* const* workspaces,
+                              const size_t* ws_bytes, int32_t nstreams, togb_batch** out) {
+  if (!progs || !workspaces || !ws_bytes || !out || n <= 0 || nstreams <= 0 || nstreams > 64)
+    return fail(TOGB_ERR_INVALID, "bad batch arguments");
+  if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
+  *out = nullptr;
+  togb_batch* b = new togb_batch();
+  b->mode = mode;
+  const int dev = progs[0]->device;
+  cudaError_t e = cudaSetDevice(dev);
+  if (e != cudaSuccess) { batch_free(b); return cuda_fail(e, "cudaSetDevice"); }
+  for (int32_t i = 0; i < n; ++i) {
+    togb_program* p = progs[i];
+    if (!p || p->device != dev || !workspaces[i]) { batch_free(b); return fail(TOGB_ERR_INVALID, "bad batch member"); }
+    for (int32_t k = 0; k < i; ++k)
+      if (progs[k] == p) { batch_free(b); return fail(TOGB_ERR_INVALID, "a program appears twice in a batch"); }
+    char* ws = (char*)(((uintptr_t)workspaces[i] + 255) & ~(uintptr_t)255);
+    const int64_t usable = (int64_t)ws_bytes[i] - (int64_t)(ws - (char*)workspaces[i]) - ws_once(p, mode);
+    const int64_t per = ws_per_slice(p, mode);
+    const int64_t B = std::min<int64_t>(usable > 0 ? usable / per : 0, std::min<int64_t>(p->num_slices, 65535));
+    if (B < 1) { batch_free(b); return fail(TOGB_ERR_OOM, "workspace of batch member " + std::to_string(i) + " smaller than one slice"); }
+    if (mode != p->cur_mode || B != p->cur_B || ws != p->cur_ws) {
+      clear_graphs(p);
+      build_descs(p, mode, ws, (int)B);
+      p->cur_mode = mode;
+      p->cur_B = (int)B;
+      p->cur_ws = ws;
+    }
+    b->progs.push_back(p);
+    b->ws.push_back(ws);
+    b->B.push_back(B);
+  }
+  const int K = std::min<int32_t>(nstreams, n);
+  b->streams.resize(K, nullptr);
+  b->joins.resize(K, nullptr);
+  if ((e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess) {
+    batch_free(b);
+    return cuda_fail(e, "batch streams");
+  }
+  for (int k = 0; k < K; ++k)
+    if ((e = cudaStreamCreateWithFlags(&b->streams[k], cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->joins[k], cudaEventDisableTiming)) != cudaSuccess) {
+      batch_free(b);
+      return cuda_fail(e, "batch streams");
+    }
+  // Capture: fork to K streams, each program's count on its stream, join back.
+  cudaGraph_t g = nullptr;
+  togb_status r = TOGB_OK;
+  if ((e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+    batch_free(b);
+    return cuda_fail(e, "batch capture");
+  }
+  e = cudaEventRecord(b->fork, b->cap);
+  for (int k = 0; e == cudaSuccess && k < K; ++k) e = cudaStreamWaitEvent(b->streams[k], b->fork, 0);
+  for (int32_t i = 0; e == cudaSuccess && r == TOGB_OK && i < n; ++i)
+    r = enqueue_count(b->progs[i], mode, b->B[i], b->streams[i % K]);
+  for (int k = 0; e == cudaSuccess && k < K; ++k) {
+    e = cudaEventRecord(b->joins[k], b->streams[k]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->cap, b->joins[k], 0);
+  }
+  cudaError_t ce = cudaStreamEndCapture(b->cap, &g);
+  if (e == cudaSuccess) e = ce;
+  if (r == TOGB_OK && e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (r != TOGB_OK || e != cudaSuccess) {
+    batch_free(b);
+    return r != TOGB_OK ? r : cuda_fail(e, "batch graph");
+  }
+  *out = b;
+  return TOGB_OK;
+}
+
+togb_status togb_batch_run(togb_batch* b, void* stream) {
+  if (!b) return fail(TOGB_ERR_INVALID, "null batch");
+  TOGB_CUDA(cudaSetDevice(b->progs[0]->device));
+  TOGB_CUDA(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+  return TOGB_OK;
+}
+
+togb_status togb_batch_results(togb_batch* b, void* stream, double* out, int32_t n) {
+  if (!b || !out) return fail(TOGB_ERR_INVALID, "null argument");
+  if (n != (int32_t)b->progs.size()) return fail(TOGB_ERR_INVALID, "n must equal the batch size");
+  for (int32_t i = 0; i < n; ++i) {
+    togb_program* p = b->progs[i];
+    const int64_t E = pow2(p->nodes[p->root].rank);
+    if (E != 1) return fail(TOGB_ERR_UNSUPPORTED, "batch results are scalar counts (root rank 0)");
+    togb_status r = togb_program_result(p, stream, out + i, nullptr, 1);
+    if (r != TOGB_OK) return r;
+  }
+  return TOGB_OK;
+}
+
+void togb_batch_destroy(togb_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->progs.empty() ? 0 : b->progs[0]->device);
+  batch_free(b);
+}
+
+}  // extern "C"
+
 togb_status togb_tensordot_f64(const double* a, int32_t ra, const double* b, int32_t rb, int32_t n_axes,
                                const int32_t* axes_a, const int32_t* axes_b, double* out, void* stream) {
   if (!a || !b || !out) return fail(TOGB_ERR_INVALID, "null tensor");

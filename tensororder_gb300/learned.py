@@ -321,3 +321,42 @@ class Selector:
             if best is None or t < best.predicted_s:
                 best = Choice(prog, [-1] * prog.num_joins, t, "flop-model")
         return best
+
+
+def workspace_per_slice(programs: Sequence[Program], mode: int, device: int = 0) -> List[float]:
+    """Device workspace bytes per slice of each program (lowered by the library)."""
+    out = []
+    for p in programs:
+        dp = runtime.DeviceProgram(p, device)
+        out.append(float(dp.info.workspace_per_slice[mode]))
+        dp.close()
+    return out
+
+
+def run_choice(choice: Choice, mode: int, repeats: int = 3, device: int = 0, max_fraction: float = 0.5,
+               max_slices: Optional[int] = None) -> Tuple[float, float]:
+    """Contract ``choice`` (its slice set and kernels); returns the count of
+    the first ``max_slices`` slices (all by default) and the median device
+    time of one pass over them in seconds."""
+    import torch
+
+    dp = runtime.DeviceProgram(choice.program, device)
+    for j, k in enumerate(choice.kernels):
+        if k >= 0:
+            dp.set_kernel(mode, j, k)
+    n = dp.num_slices if max_slices is None else min(dp.num_slices, max_slices)
+    ws = dp.allocate_workspace(mode, n, max_fraction=max_fraction)
+    stream = torch.cuda.current_stream(device)
+    times = []
+    for _ in range(repeats + 1):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        dp.reset(stream)
+        a.record(stream)
+        dp.run(mode, 0, n, workspace=ws, stream=stream)
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b) * 1e-3)
+    count = float(dp.result(stream).reshape(-1)[0])
+    dp.close()
+    return count, float(np.median(times[1:]))

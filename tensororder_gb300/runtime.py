@@ -74,6 +74,8 @@ EXPORTS = [
     "togb_program_reset", "togb_program_run", "togb_program_result", "togb_program_set_timing",
     "togb_program_join_times", "togb_program_destroy", "togb_tensordot_f64", "togb_probe_peak",
     "togb_contract_static_f64", "togb_program_joins", "togb_program_set_kernel", "togb_program_kernel_allowed",
+    "togb_mlp_param_count", "togb_mlp_scratch_floats", "togb_mlp_forward", "togb_mlp_loss_grad", "togb_mlp_adam",
+    "togb_batch_create", "togb_batch_run", "togb_batch_results", "togb_batch_destroy",
 ]
 
 KERNEL_NAMES = {0: "direct", 1: "tiled", 2: "reduce", 3: "tensor"}
@@ -113,8 +115,15 @@ def lib():
     L.togb_program_joins.argtypes = [c_void, ctypes.c_int, _i32p, ctypes.c_int32]
     L.togb_program_set_kernel.argtypes = [c_void, ctypes.c_int, ctypes.c_int32, ctypes.c_int32]
     L.togb_program_kernel_allowed.argtypes = [c_void, ctypes.c_int, ctypes.c_int32, ctypes.c_int32, _i32p]
+    L.togb_batch_create.argtypes = [ctypes.POINTER(c_void), ctypes.c_int32, ctypes.c_int, ctypes.POINTER(c_void),
+                                    ctypes.POINTER(ctypes.c_size_t), ctypes.c_int32, ctypes.POINTER(c_void)]
+    L.togb_batch_run.argtypes = [c_void, c_void]
+    L.togb_batch_results.argtypes = [c_void, c_void, _f64p, ctypes.c_int32]
+    L.togb_batch_destroy.argtypes = [c_void]
+    L.togb_batch_destroy.restype = None
     for name in EXPORTS:
-        if name not in ("togb_version", "togb_last_error", "togb_program_destroy"):
+        if name not in ("togb_version", "togb_last_error", "togb_program_destroy", "togb_batch_destroy") \
+                and not name.startswith("togb_mlp"):
             getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
