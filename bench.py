@@ -281,9 +281,8 @@ def main():
                  "share_of_step": float(jt_split[top] / jt_split.sum()),
                  "algorithmic_bytes": top_bytes, "traffic": None})
     if (mb, nb, kb, kern) == (8, 11, 9, 3):
-        # DRAM read + write of this join in the ncu capture of its first 32 slices
-        # (profiles/k_umma_ws_wvc220_32slices.md: 151.1 + 36.6 MB), scaled to the
-        # slices of one full launch.
+        # DRAM read + write of this join in an ncu capture (--set full) of its
+        # first 32 slices, 151.1 + 36.6 MB, scaled to the slices of one launch.
         roof["traffic"] = (151.133184e6 + 36.597504e6) * runs / 32
         roof["traffic_source"] = "ncu capture of 32 slices scaled by %d/32" % runs
 
