@@ -22,6 +22,9 @@
 //    on the IEEE bits, valid because every entry is >= 0).
 #include <cuda_runtime.h>
 
+#include <cstring>
+#include <type_traits>
+
 #include "togb_internal.h"
 #include "togb_device.cuh"
 
@@ -460,6 +463,83 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const __grid_constant__ Joi
   }
 }
 
+// k_reduce for operands whose K axis is contiguous (unit stride, offsets
+// aligned to 16 bytes, no leaf residual): each thread reads 16-byte vectors of
+// both operands, four vectors deep, and adds 16-term partials into a
+// compensated sum; a pairwise tree across the CTA finishes the entry.
+template <int MODE, class T>
+__global__ void __launch_bounds__(kThreads) k_reduce_vec(const __grid_constant__ JoinDesc jd,
+                                                         const int64_t* __restrict__ d_s0, int nslices) {
+  constexpr int VW = 16 / sizeof(T);  // elements per vector
+  using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  __shared__ double red_hi[kThreads / 32];
+  __shared__ double red_lo[kThreads / 32];
+  const int mnb = jd.mb + jd.nb;
+  const int64_t blk = blockIdx.x + (int64_t)blockIdx.y * gridDim.x;
+  const int b = (int)(blk >> mnb);
+  if (b >= nslices) return;
+  const uint64_t mn = (uint64_t)blk & ((1ull << mnb) - 1);
+  const uint64_t m = mn >> jd.nb, n = mn & ((1ull << jd.nb) - 1);
+  const int64_t s = (d_s0 ? *d_s0 : 0) + b;
+  const int tid = threadIdx.x;
+  const V* __restrict__ A = reinterpret_cast<const V*>((const T*)jd.a.ptr + slice_offset(jd.a, b, s) + dep(jd.a.r_outer, m));
+  const V* __restrict__ B = reinterpret_cast<const V*>((const T*)jd.b.ptr + slice_offset(jd.b, b, s) + dep(jd.b.r_outer, n));
+  const int64_t nv = (1ll << jd.kb) / VW;
+  int sa = 0, sb = 0;
+  T fa = 1, fb = 1;
+  if (MODE == 1) {
+    sa = op_shift(jd.a, b);
+    sb = op_shift(jd.b, b);
+    fa = (T)pow2f(sa);
+    fb = (T)pow2f(sb);
+  }
+  T sum = 0, comp = 0;
+  constexpr int U = 4;
+  for (int64_t v0 = tid; v0 < nv; v0 += (int64_t)U * kThreads) {
+    V av[U], bv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t v = v0 + (int64_t)u * kThreads;
+      if (v < nv) {
+        av[u] = A[v];
+        bv[u] = B[v];
+      } else {
+        memset(&av[u], 0, sizeof(V));
+        memset(&bv[u], 0, sizeof(V));
+      }
+    }
+    T part = 0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const T* x = reinterpret_cast<const T*>(&av[u]);
+      const T* y = reinterpret_cast<const T*>(&bv[u]);
+#pragma unroll
+      for (int q = 0; q < VW; ++q) part = fma(x[q] * fa, y[q] * fb, part);
+    }
+    const T t = sum + part;
+    comp += fabs(sum) >= fabs(part) ? (sum - t) + part : (part - t) + sum;
+    sum = t;
+  }
+  double hi = (double)sum, lo = (double)comp;
+  for (int off = 16; off > 0; off >>= 1) {
+    hi += __shfl_xor_sync(0xffffffffu, hi, off);
+    lo += __shfl_xor_sync(0xffffffffu, lo, off);
+  }
+  if ((tid & 31) == 0) { red_hi[tid >> 5] = hi; red_lo[tid >> 5] = lo; }
+  __syncthreads();
+  if (tid == 0) {
+    double h = 0.0, l = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) { h += red_hi[w]; l += red_lo[w]; }
+    const double total = h + l;
+    T* C = (T*)jd.c_ptr + (int64_t)b * jd.c_batch_stride + dep(jd.r_cm, m) + dep(jd.r_cn, n);
+    *C = (T)total;
+    if (MODE == 1) {
+      atomicMax(&jd.c_max[b], __float_as_uint((float)total));
+      if (mn == 0) jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - sa - sb;
+    }
+  }
+}
+
 // Compensated (Neumaier) accumulation of every slice's root tensor, in slice
 // order, into the FP64 accumulator.
 template <int MODE, class T>
@@ -531,6 +611,20 @@ __global__ void __launch_bounds__(kThreads) k_probe_dmma(double* out, int iters)
   if (r == -1.0) out[0] = r;
 }
 
+// An operand k_reduce_vec can read: unit-stride K, no leaf residual, and every
+// possible base offset (slice, outer index) and the pointer 16-byte aligned.
+bool reduce_vec_ok(const OpDesc& o, int mode) {
+  const int64_t vw = mode == 0 ? 2 : 4;
+  if (o.ptr_lo) return false;
+  if (o.r_k.n != 1 || o.r_k.src[0] != 0 || o.r_k.dst[0] != 0) return false;
+  if (((uintptr_t)o.ptr & 15) != 0 || o.batch_stride % vw != 0) return false;
+  for (int j = 0; j < o.n_slice_terms; ++j)
+    if (o.slice_stride[j] % vw != 0) return false;
+  for (int i = 0; i < o.outer_bits; ++i)
+    if (o.s_outer[i] % vw != 0) return false;
+  return true;
+}
+
 int grid_for(int64_t work) {
   const int64_t blocks = (work + kThreads - 1) / kThreads;
   const int64_t cap = 152 * 32;
@@ -557,8 +651,14 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
     const unsigned gx = (unsigned)(blocks < 65536 ? blocks : 65536);
     const unsigned gy = (unsigned)((blocks + gx - 1) / gx);
     if (gy > 65535) return cudaErrorInvalidValue;
-    if (mode == 0) k_reduce<0, double><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
-    else k_reduce<1, float><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
+    const bool vec = reduce_vec_ok(jd.a, mode) && reduce_vec_ok(jd.b, mode) && jd.kb >= 10;
+    if (vec) {
+      if (mode == 0) k_reduce_vec<0, double><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
+      else k_reduce_vec<1, float><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
+    } else {
+      if (mode == 0) k_reduce<0, double><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
+      else k_reduce<1, float><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
+    }
   } else {
     const int mnb = jd.mb + jd.nb;
     const int vec = mnb >= 2 ? 4 : 1;
