@@ -92,6 +92,15 @@ togb_status togb_program_create(const togb_program_desc* desc, int device, togb_
 
 togb_status togb_program_info_get(const togb_program* prog, togb_program_info* info);
 
+/* Lower and plan a program on the host only (no device, no leaf values
+ * needed), for inspecting the plan: togb_program_info_get,
+ * togb_program_joins, togb_program_kernel_allowed and togb_program_describe
+ * work on it; running it does not.  Destroy with togb_program_destroy. */
+togb_status togb_program_create_host(const togb_program_desc* desc, togb_program** out);
+/* Text description of join `join` in `mode`: GEMM extents, kernel, operand
+ * and output strides and their bit runs (host-only programs). */
+togb_status togb_program_describe(togb_program* prog, int mode, int32_t join, char* buf, size_t n);
+
 /* Zero the device-side slice accumulator (compensated FP64 sum). */
 togb_status togb_program_reset(togb_program* prog, void* stream);
 

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <string>
@@ -169,6 +170,7 @@ struct togb_program {
   std::map<int, cudaGraphExec_t> graphs;  // by chunk slice count
   bool use_graphs = true;
   bool timing = false;
+  bool host_only = false;  // lowered for inspection only; owns no device memory
   std::vector<float> join_ms;
 };
 
@@ -827,6 +829,53 @@ togb_status togb_program_create(const togb_program_desc* d, int device, togb_pro
   return TOGB_OK;
 }
 
+togb_status togb_program_create_host(const togb_program_desc* d, togb_program** out) {
+  if (!d || !out) return fail(TOGB_ERR_INVALID, "null argument");
+  int64_t voff = 0;
+  togb_program* p = nullptr;
+  togb_status st = lower_host(d, -1, &p, &voff);
+  if (st != TOGB_OK) return st;
+  p->host_only = true;
+  *out = p;
+  return TOGB_OK;
+}
+
+togb_status togb_program_describe(togb_program* p, int mode, int32_t join, char* buf, size_t n) {
+  if (!p || !buf || n == 0) return fail(TOGB_ERR_INVALID, "null argument");
+  if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
+  if (join < 0 || join >= (int32_t)p->joins.size()) return fail(TOGB_ERR_INVALID, "join index out of range");
+  if (p->cur_mode != mode || !p->host_only) {
+    if (!p->host_only) return fail(TOGB_ERR_UNSUPPORTED, "describe works on host-only programs");
+    // Descriptors against a null workspace: offsets are what matters here.
+    build_descs(p, mode, nullptr, 1);
+    p->cur_mode = mode;
+  }
+  const JoinDesc& jd = p->jds[join];
+  const Node& J = p->nodes[p->joins[join]];
+  std::string s = "join " + std::to_string(join) + " mnk " + std::to_string(jd.mb) + " " + std::to_string(jd.nb) +
+                  " " + std::to_string(jd.kb) + " kernel " + std::to_string(join_kernel(p, J, mode)) +
+                  " per_slice " + std::to_string(J.dep ? 1 : 0) + " c_natural " + std::to_string(jd.c_natural) + "\n";
+  auto strides = [&](const char* name, const int64_t* v, int nb) {
+    s += name;
+    for (int i = 0; i < nb; ++i) s += " " + std::to_string(v[i]);
+    s += "\n";
+  };
+  for (int w = 0; w < 2; ++w) {
+    const OpDesc& o = w ? jd.b : jd.a;
+    s += w ? "B" : "A";
+    s += std::string(" leaf ") + (o.exp_ptr || o.batch_stride ? "0" : "1") + " batch_stride " +
+         std::to_string(o.batch_stride) + " k_fast " + std::to_string(o.k_fast) + " runs_outer " +
+         std::to_string(o.r_outer.n) + " runs_k " + std::to_string(o.r_k.n) + "\n";
+    strides(w ? "  B s_outer" : "  A s_outer", o.s_outer, o.outer_bits);
+    strides(w ? "  B s_k" : "  A s_k", o.s_k, o.k_bits);
+  }
+  strides("C s_m", jd.c_s_m, jd.mb);
+  strides("C s_n", jd.c_s_n, jd.nb);
+  s += "C runs_inv_m " + std::to_string(jd.r_inv_m.n) + " runs_inv_n " + std::to_string(jd.r_inv_n.n) + "\n";
+  std::snprintf(buf, n, "%s", s.c_str());
+  return TOGB_OK;
+}
+
 togb_status togb_program_info_get(const togb_program* p, togb_program_info* info) {
   if (!p || !info) return fail(TOGB_ERR_INVALID, "null argument");
   info->num_slices = p->num_slices;
@@ -848,6 +897,7 @@ togb_status togb_program_info_get(const togb_program* p, togb_program_info* info
 
 togb_status togb_program_reset(togb_program* p, void* stream) {
   if (!p) return fail(TOGB_ERR_INVALID, "null program");
+  if (p->host_only) return fail(TOGB_ERR_UNSUPPORTED, "host-only program: create it with togb_program_create to run it");
   TOGB_CUDA(cudaSetDevice(p->device));
   const int64_t E = pow2(p->nodes[p->root].rank);
   TOGB_CUDA(cudaMemsetAsync(p->d_acc, 0, 2 * E * 8, (cudaStream_t)stream));
@@ -911,6 +961,7 @@ togb_status togb_program_join_times(togb_program* p, float* ms, int32_t n) {
 togb_status togb_program_run(togb_program* p, int mode, int64_t begin, int64_t end, void* workspace,
                              size_t ws_bytes, void* stream_v) {
   if (!p) return fail(TOGB_ERR_INVALID, "null program");
+  if (p->host_only) return fail(TOGB_ERR_UNSUPPORTED, "host-only program: create it with togb_program_create to run it");
   if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
   if (begin < 0 || end > p->num_slices || begin > end) return fail(TOGB_ERR_INVALID, "slice range out of bounds");
   if (begin == end) return TOGB_OK;
@@ -961,6 +1012,7 @@ togb_status togb_program_run(togb_program* p, int mode, int64_t begin, int64_t e
 
 togb_status togb_program_result(togb_program* p, void* stream, double* out, double* comp, int64_t n) {
   if (!p || !out) return fail(TOGB_ERR_INVALID, "null argument");
+  if (p->host_only) return fail(TOGB_ERR_UNSUPPORTED, "host-only program has no result");
   const int64_t E = pow2(p->nodes[p->root].rank);
   if (n != E) return fail(TOGB_ERR_INVALID, "result size does not match the root tensor");
   TOGB_CUDA(cudaSetDevice(p->device));
@@ -982,6 +1034,10 @@ togb_status togb_program_result(togb_program* p, void* stream, double* out, doub
 
 void togb_program_destroy(togb_program* p) {
   if (!p) return;
+  if (p->host_only) {
+    delete p;
+    return;
+  }
   cudaSetDevice(p->device);
   clear_graphs(p);
   cudaFree(p->d_leaf64);

@@ -76,6 +76,7 @@ EXPORTS = [
     "togb_contract_static_f64", "togb_program_joins", "togb_program_set_kernel", "togb_program_kernel_allowed",
     "togb_mlp_param_count", "togb_mlp_scratch_floats", "togb_mlp_forward", "togb_mlp_loss_grad", "togb_mlp_adam",
     "togb_batch_create", "togb_batch_run", "togb_batch_results", "togb_batch_destroy",
+    "togb_program_create_host", "togb_program_describe",
 ]
 
 KERNEL_NAMES = {0: "direct", 1: "tiled", 2: "reduce", 3: "tensor"}
@@ -118,6 +119,8 @@ def lib():
     L.togb_batch_create.argtypes = [ctypes.POINTER(c_void), ctypes.c_int32, ctypes.c_int, ctypes.POINTER(c_void),
                                     ctypes.POINTER(ctypes.c_size_t), ctypes.c_int32, ctypes.POINTER(c_void)]
     L.togb_batch_run.argtypes = [c_void, c_void]
+    L.togb_program_create_host.argtypes = [ctypes.POINTER(ProgramDesc), ctypes.POINTER(c_void)]
+    L.togb_program_describe.argtypes = [c_void, ctypes.c_int, ctypes.c_int32, ctypes.c_char_p, ctypes.c_size_t]
     L.togb_batch_results.argtypes = [c_void, c_void, _f64p, ctypes.c_int32]
     L.togb_batch_destroy.argtypes = [c_void]
     L.togb_batch_destroy.restype = None
@@ -145,27 +148,80 @@ def _stream_handle(stream):
     return ctypes.c_void_p(stream.cuda_stream)
 
 
+class _Desc:
+    """A togb_program_desc with the arrays it points into kept alive."""
+
+    def __init__(self, program: Program, with_values=True):
+        leaves = program.leaves
+        self.ranks = np.array([l.rank for l in leaves], dtype=np.int32)
+        self.axes = np.array([a for l in leaves for a in l.axes] or [0], dtype=np.int32)
+        if with_values:
+            vals = [l.parent().ravel() for l in leaves]
+            self.values = np.ascontiguousarray(np.concatenate(vals) if vals else np.zeros(1), dtype=np.float64)
+        else:
+            self.values = None
+        self.tokens = np.array(program.postorder, dtype=np.int32)
+        self.gsize = np.array([len(g) for g in program.slice_groups] or [0], dtype=np.int32)
+        self.gedges = np.array([e for g in program.slice_groups for e in g] or [0], dtype=np.int32)
+        self.desc = ProgramDesc(
+            len(leaves), self.ranks.ctypes.data_as(_i32p), self.axes.ctypes.data_as(_i32p),
+            self.values.ctypes.data_as(_f64p) if self.values is not None else None, len(self.tokens),
+            self.tokens.ctypes.data_as(_i32p), len(program.slice_groups), self.gsize.ctypes.data_as(_i32p),
+            self.gedges.ctypes.data_as(_i32p))
+
+
+class HostProgram:
+    """A program lowered and planned on the host only, for inspection
+    (``togb_program_create_host``): joins, allowed kernels, layouts."""
+
+    def __init__(self, program: Program):
+        self.program = program
+        self._d = _Desc(program, with_values=False)
+        handle = ctypes.c_void_p()
+        check(lib().togb_program_create_host(ctypes.byref(self._d.desc), ctypes.byref(handle)))
+        self._h = handle
+        info = ProgramInfo()
+        check(lib().togb_program_info_get(self._h, ctypes.byref(info)))
+        self.info = info
+
+    def joins(self, mode):
+        n = int(self.info.num_joins)
+        out = np.zeros((max(n, 1), 5), dtype=np.int32)
+        check(lib().togb_program_joins(self._h, int(mode), out.ctypes.data_as(_i32p), n))
+        return out[:n]
+
+    def describe(self, mode, join):
+        buf = ctypes.create_string_buffer(8192)
+        check(lib().togb_program_describe(self._h, int(mode), int(join), buf, 8192))
+        return buf.value.decode()
+
+    def kernel_allowed(self, mode, join, kernel):
+        out = ctypes.c_int32()
+        check(lib().togb_program_kernel_allowed(self._h, int(mode), int(join), int(kernel), ctypes.byref(out)))
+        return bool(out.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().togb_program_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class DeviceProgram:
     """A program lowered and planned by libtogb, with its leaves on the device."""
 
     def __init__(self, program: Program, device: int = 0):
         self.program = program
         self.device = device
-        leaves = program.leaves
-        self._ranks = np.array([l.rank for l in leaves], dtype=np.int32)
-        self._axes = np.array([a for l in leaves for a in l.axes] or [0], dtype=np.int32)
-        vals = [l.parent().ravel() for l in leaves]
-        self._values = np.ascontiguousarray(np.concatenate(vals) if vals else np.zeros(1), dtype=np.float64)
-        self._tokens = np.array(program.postorder, dtype=np.int32)
-        self._gsize = np.array([len(g) for g in program.slice_groups] or [0], dtype=np.int32)
-        self._gedges = np.array([e for g in program.slice_groups for e in g] or [0], dtype=np.int32)
-        desc = ProgramDesc(
-            len(leaves), self._ranks.ctypes.data_as(_i32p), self._axes.ctypes.data_as(_i32p),
-            self._values.ctypes.data_as(_f64p), len(self._tokens), self._tokens.ctypes.data_as(_i32p),
-            len(program.slice_groups), self._gsize.ctypes.data_as(_i32p), self._gedges.ctypes.data_as(_i32p),
-        )
+        self._d = _Desc(program)
+        self._values = self._d.values
         handle = ctypes.c_void_p()
-        check(lib().togb_program_create(ctypes.byref(desc), device, ctypes.byref(handle)))
+        check(lib().togb_program_create(ctypes.byref(self._d.desc), device, ctypes.byref(handle)))
         self._h = handle
         info = ProgramInfo()
         check(lib().togb_program_info_get(self._h, ctypes.byref(info)))
