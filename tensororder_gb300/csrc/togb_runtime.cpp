@@ -272,10 +272,31 @@ void plan_layouts(togb_program* p) {
     const Node& R = p->nodes[J.right];
     std::vector<int> kappa = J.k_lsb;
     const Node* leaf = L.leaf >= 0 ? &L : (R.leaf >= 0 ? &R : nullptr);
-    if (leaf)
+    // A GEMM-shaped operand producer writes its tile rows fastest when its
+    // column axes are its output's lowest address bits (row-major tiles).  The
+    // shared axes sit at the bottom of both operands, so order them for the
+    // larger such producer: its column axes first (in its own order), then the
+    // rest by its natural strides.
+    const Node* fav = nullptr;
+    for (const Node* X : {&L, &R})
+      if (X->leaf < 0 && X->kernel == togb::K_TILED && (!fav || X->rank > fav->rank)) fav = X;
+    if (fav) {
+      const bool swapped = fav->m_lsb.size() < 7 && fav->n_lsb.size() > fav->m_lsb.size();
+      const std::vector<int>& cols = swapped ? fav->m_lsb : fav->n_lsb;
+      std::vector<int> lsb;
+      for (int e : cols)
+        if (in(kappa, e)) lsb.push_back(e);
+      std::vector<int> rest;
+      for (int e : kappa)
+        if (!in(lsb, e)) rest.push_back(e);
+      std::sort(rest.begin(), rest.end(), [fav](int a, int b) { return fav->stride.at(a) < fav->stride.at(b); });
+      lsb.insert(lsb.end(), rest.begin(), rest.end());
+      kappa.assign(lsb.rbegin(), lsb.rend());  // most significant first
+    } else if (leaf) {
       std::sort(kappa.begin(), kappa.end(), [leaf](int a, int b) { return leaf->stride.at(a) > leaf->stride.at(b); });
-    else
+    } else {
       std::sort(kappa.begin(), kappa.end());
+    }
     if (L.leaf < 0) {
       req[J.left] = mu;
       req[J.left].insert(req[J.left].end(), kappa.begin(), kappa.end());

@@ -26,11 +26,14 @@
 //
 // The kernel is persistent (one CTA per SM walking the tiles), so the next
 // tile's loads, conversions and first MMAs overlap the current tile's
-// epilogue.  Each read-out thread owns one output row.  When the tile's n bits
-// are the output's lowest address bits, every read-out warp transposes its 32
-// rows through a private shared-memory area so that each store instruction
-// writes whole 128-byte row segments; otherwise lanes store their rows'
-// columns directly (consecutive rows, coalesced when the m bits are lowest).
+// epilogue.  Each read-out thread owns one output row.  When the tile's two
+// lowest n bits are the output's two lowest address bits, every read-out warp
+// transposes its 32 rows through a private shared-memory area and stores
+// 16-byte vectors, four rows of eight per instruction (whole 128-byte row
+// segments when the first five n bits are contiguous); otherwise lanes store
+// their rows' columns directly (coalesced when the m bits are lowest).  The
+// layout planner orders a GEMM consumer's shared axes so that the larger of its
+// GEMM-shaped producers gets such a layout.
 // The slice maximum and exponent are recorded like in the other split-form
 // kernels.
 //
@@ -254,10 +257,10 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
     const int row = 32 * q + lane;
     const int col0 = hf * HALF;
     const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)col0;
-    // Row-major float4 stores when the tile's n bits are the output's lowest address bits.
-    const int nbits_tile = jd.nb < (BN == 128 ? 7 : 6) ? jd.nb : (BN == 128 ? 7 : 6);
-    bool rowmajor = nbits_tile >= 2;
-    for (int i = 0; i < nbits_tile; ++i) rowmajor = rowmajor && jd.c_s_n[i] == (1ll << i);
+    // Staged float4 stores when the tile's two lowest n bits are the output's
+    // two lowest address bits (four columns form one 16-byte vector); the
+    // vectors of a row are then placed through the column offset table.
+    const bool rowmajor = jd.nb >= 2 && jd.c_s_n[0] == 1 && jd.c_s_n[1] == 2;
     float4* wst = reinterpret_cast<float4*>(smem + NR * L::RAW + NC * L::CONV) + (warp - 8) * 256;  // 32 rows x 8 float4
     int gw = 0;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -303,7 +306,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
       if (rowmajor) {
         // 32 columns at a time through this warp's staging area: each lane
         // writes its row's eight float4, then one store instruction covers four
-        // full 128-byte row segments (float4 slots XOR-swizzled by the row).
+        // rows of eight vectors -- whole 128-byte segments when the first five
+        // n bits are contiguous (float4 slots XOR-swizzled by the row).
 #pragma unroll
         for (int p = 0; p < HALF; p += 32) {
 #pragma unroll
@@ -315,7 +319,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
           for (int k = 0; k < 8; ++k) {
             const int r = (lane >> 3) + 4 * k, c = lane & 7, gr = 32 * q + r;
             if (gr < mlim && col0 + p + 4 * c < nlim)
-              *reinterpret_cast<float4*>(C + tCm[gr] + col0 + p + 4 * c) = wst[r * 8 + (c ^ (r & 7))];
+              *reinterpret_cast<float4*>(C + tCm[gr] + tCn[col0 + p + 4 * c]) = wst[r * 8 + (c ^ (r & 7))];
           }
           __syncwarp();
         }
