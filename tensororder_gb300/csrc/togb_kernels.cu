@@ -198,6 +198,142 @@ __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ Joi
   }
 }
 
+// Thread-per-output kernel with staged operands, for short K (KK <= 16).
+// Each CTA takes tiles of 2^T consecutive output addresses of one slice.  The
+// T lowest address bits belong to lm bits of m and ln bits of n (lm + ln = T),
+// so a tile reads just 2^lm rows of A and 2^ln rows of B: the CTA loads those
+// rows (K values each) into shared memory once, then every thread computes
+// four consecutive outputs from shared memory and stores them as one vector.
+// Output addresses are dense per slice, so a tile is one contiguous run.
+struct StageInfo {
+  int T, lm, ln;
+  int a_row_bits[12];   // A s_outer index of the r-th staged m bit
+  int b_row_bits[12];
+};
+
+template <int MODE, class T, int KK>
+__global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constant__ JoinDesc jd,
+                                                            const __grid_constant__ StageInfo si,
+                                                            const int64_t* __restrict__ d_s0, int nslices) {
+  extern __shared__ float sm_dyn[];
+  __shared__ int32_t offA[1 << 12], offB[1 << 12];
+  __shared__ uint16_t IA[2][64], IB[2][64];
+  const int TB = si.T;
+  const int rowsA = 1 << si.lm, rowsB = 1 << si.ln;
+  T* As = reinterpret_cast<T*>(sm_dyn);
+  T* Bs = As + (size_t)rowsA * KK;
+  float* Alo = reinterpret_cast<float*>(Bs + (size_t)rowsB * KK);
+  float* Blo = Alo + (jd.a.ptr_lo ? (size_t)rowsA * KK : 0);
+  const int mnb = jd.mb + jd.nb;
+  const uint64_t nmask = (1ull << jd.nb) - 1;
+  const uint64_t lowmask = (1ull << TB) - 1;
+  // Compaction tables: tile-local address q -> staged row of A and of B.
+  for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+    const int lvl = i >> 6, x = i & 63;
+    const uint64_t q = ((uint64_t)x << (6 * lvl)) & lowmask;
+    const uint64_t m = jd.c_natural ? (q >> jd.nb) : (uint64_t)dep(jd.r_inv_m, q);
+    const uint64_t n = jd.c_natural ? (q & nmask) : (uint64_t)dep(jd.r_inv_n, q);
+    uint32_t ra = 0, rb = 0;
+    for (int r = 0; r < si.lm; ++r) ra |= (uint32_t)((m >> si.a_row_bits[r]) & 1) << r;
+    for (int r = 0; r < si.ln; ++r) rb |= (uint32_t)((n >> si.b_row_bits[r]) & 1) << r;
+    IA[lvl][x] = (uint16_t)ra;
+    IB[lvl][x] = (uint16_t)rb;
+  }
+  // Offsets of the staged rows relative to the tile's base row.
+  for (int r = threadIdx.x; r < rowsA; r += blockDim.x) {
+    int64_t o = 0;
+    for (int b = 0; b < si.lm; ++b)
+      if ((r >> b) & 1) o += jd.a.s_outer[si.a_row_bits[b]];
+    offA[r] = (int32_t)o;
+  }
+  for (int r = threadIdx.x; r < rowsB; r += blockDim.x) {
+    int64_t o = 0;
+    for (int b = 0; b < si.ln; ++b)
+      if ((r >> b) & 1) o += jd.b.s_outer[si.b_row_bits[b]];
+    offB[r] = (int32_t)o;
+  }
+  const T* __restrict__ A = (const T*)jd.a.ptr;
+  const T* __restrict__ B = (const T*)jd.b.ptr;
+  T* __restrict__ C = (T*)jd.c_ptr;
+  const int64_t s0 = d_s0 ? *d_s0 : 0;
+  const int64_t tiles_per_slice = 1ll << (mnb - TB);
+  const int64_t ntiles = (int64_t)nslices * tiles_per_slice;
+  const int per_thread = (1 << TB) / (4 * kThreads);  // vector groups per thread (>= 1)
+  __syncthreads();
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int b = (int)(t / tiles_per_slice);
+    const uint64_t qh = (uint64_t)(t % tiles_per_slice) << TB;  // tile base address within the slice
+    const int64_t s = s0 + b;
+    const uint64_t mh = jd.c_natural ? (qh >> jd.nb) : (uint64_t)dep(jd.r_inv_m, qh);
+    const uint64_t nh = jd.c_natural ? (qh & nmask) : (uint64_t)dep(jd.r_inv_n, qh);
+    const int64_t baseA = slice_offset(jd.a, b, s) + dep(jd.a.r_outer, mh);
+    const int64_t baseB = slice_offset(jd.b, b, s) + dep(jd.b.r_outer, nh);
+    int sa = 0, sb = 0;
+    float fa = 1.f, fb = 1.f;
+    if (MODE == 1) {
+      sa = op_shift(jd.a, b);
+      sb = op_shift(jd.b, b);
+      fa = pow2f(sa);
+      fb = pow2f(sb);
+    }
+    __syncthreads();  // the previous tile's reads of the staged rows are done
+    for (int e = threadIdx.x; e < rowsA * KK; e += blockDim.x) {
+      const int r = e / KK, k = e - r * KK;
+      const int64_t o = baseA + offA[r] + jd.a.ktab[k];
+      As[e] = A[o];
+      if (MODE == 1 && jd.a.ptr_lo) Alo[e] = ((const float*)jd.a.ptr_lo)[o];
+    }
+    for (int e = threadIdx.x; e < rowsB * KK; e += blockDim.x) {
+      const int r = e / KK, k = e - r * KK;
+      const int64_t o = baseB + offB[r] + jd.b.ktab[k];
+      Bs[e] = B[o];
+      if (MODE == 1 && jd.b.ptr_lo) Blo[e] = ((const float*)jd.b.ptr_lo)[o];
+    }
+    __syncthreads();
+    uint32_t bits = 0;
+    for (int i = 0; i < per_thread; ++i) {
+      const int q0 = 4 * (threadIdx.x + kThreads * i);
+      T out[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int q = q0 + j;
+        const int ra = IA[0][q & 63] | IA[1][(q >> 6) & 63];
+        const int rb = IB[0][q & 63] | IB[1][(q >> 6) & 63];
+        const T* ar = As + ra * KK;
+        const T* br = Bs + rb * KK;
+        if (MODE == 1) {
+          float f = 0.f;
+          if (jd.a.ptr_lo) {
+            const float* al = Alo + ra * KK;
+#pragma unroll
+            for (int k = 0; k < KK; ++k) f = fmaf(al[k] * fa, (float)br[k] * fb, f);
+          }
+          if (jd.b.ptr_lo) {
+            const float* bl = Blo + rb * KK;
+#pragma unroll
+            for (int k = 0; k < KK; ++k) f = fmaf((float)ar[k] * fa, bl[k] * fb, f);
+          }
+#pragma unroll
+          for (int k = 0; k < KK; ++k) f = fmaf((float)ar[k] * fa, (float)br[k] * fb, f);
+          out[j] = (T)f;
+          bits = max(bits, __float_as_uint(f));
+        } else {
+          T acc = 0;
+#pragma unroll
+          for (int k = 0; k < KK; ++k) acc = fma(ar[k], br[k], acc);
+          out[j] = acc;
+        }
+      }
+      store_vec(C + (int64_t)b * jd.c_batch_stride + qh + q0, out);
+    }
+    if (MODE == 1) {
+      for (int off = 16; off > 0; off >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, off));
+      if ((threadIdx.x & 31) == 0) atomicMax(&jd.c_max[b], bits);
+      if (qh == 0 && threadIdx.x == 0) jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - sa - sb;
+    }
+  }
+}
+
 __device__ __forceinline__ void load4(const float* p, float* v) {
   const float4 x = *reinterpret_cast<const float4*>(p);
   v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
@@ -631,6 +767,55 @@ int grid_for(int64_t work) {
   return (int)(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
 }
 
+// The staged thread-per-output variant applies to K <= 16 when a tile of 2^T
+// (T in [10, 12]) output addresses touches at least 4 rows of each operand
+// (rows are reused) and the staged rows fit 64 KB.  Returns true when launched.
+bool launch_staged(int mode, const JoinDesc& jd, const int64_t* s0, int nslices, cudaStream_t st) {
+  const int mnb = jd.mb + jd.nb;
+  if (jd.kb > 4 || mnb < 10) return false;
+  const int K = 1 << jd.kb;
+  const size_t es = mode == 0 ? 8 : 4;
+  StageInfo si{};
+  for (int T = mnb < 12 ? mnb : 12; T >= 10; --T) {
+    int lm = 0, ln = 0;
+    for (int i = 0; i < jd.mb; ++i)
+      if (jd.c_s_m[i] < (1ll << T)) si.a_row_bits[lm++] = i;
+    for (int i = 0; i < jd.nb; ++i)
+      if (jd.c_s_n[i] < (1ll << T)) si.b_row_bits[ln++] = i;
+    if (lm + ln != T || lm < 2 || ln < 2) continue;
+    size_t bytes = ((size_t)1 << lm) * K * es + ((size_t)1 << ln) * K * es;
+    if (mode == 1) bytes += (jd.a.ptr_lo ? ((size_t)1 << lm) * K * 4 : 0) + (jd.b.ptr_lo ? ((size_t)1 << ln) * K * 4 : 0);
+    if (bytes > 64 * 1024) continue;
+    si.T = T;
+    si.lm = lm;
+    si.ln = ln;
+    const int64_t tiles = (int64_t)nslices << (mnb - T);
+    const int grid = (int)(tiles < 152 * 4 ? tiles : 152 * 4);
+#define TOGB_STAGED(KK)                                                                                   \
+    {                                                                                                     \
+      if (mode == 0) {                                                                                    \
+        cudaFuncSetAttribute(k_direct_staged<0, double, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             64 * 1024);                                                                  \
+        k_direct_staged<0, double, KK><<<grid, kThreads, bytes, st>>>(jd, si, s0, nslices);                \
+      } else {                                                                                            \
+        cudaFuncSetAttribute(k_direct_staged<1, float, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                             64 * 1024);                                                                  \
+        k_direct_staged<1, float, KK><<<grid, kThreads, bytes, st>>>(jd, si, s0, nslices);                 \
+      }                                                                                                   \
+    }
+    switch (jd.kb) {
+      case 0: TOGB_STAGED(1) break;
+      case 1: TOGB_STAGED(2) break;
+      case 2: TOGB_STAGED(4) break;
+      case 3: TOGB_STAGED(8) break;
+      default: TOGB_STAGED(16) break;
+    }
+#undef TOGB_STAGED
+    return true;
+  }
+  return false;
+}
+
 }  // namespace
 
 cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t* s0, int nslices,
@@ -659,6 +844,8 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
       if (mode == 0) k_reduce<0, double><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
       else k_reduce<1, float><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
     }
+  } else if (launch_staged(mode, jd, s0, nslices, st)) {
+    // short-K join with reused operand rows: staged variant launched
   } else {
     const int mnb = jd.mb + jd.nb;
     const int vec = mnb >= 2 ? 4 : 1;
