@@ -215,15 +215,17 @@ template <int MODE, class T, int KK>
 __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constant__ JoinDesc jd,
                                                             const __grid_constant__ StageInfo si,
                                                             const int64_t* __restrict__ d_s0, int nslices) {
-  extern __shared__ float sm_dyn[];
-  __shared__ int32_t offA[1 << 12], offB[1 << 12];
+  extern __shared__ __align__(16) unsigned char sm_dyn[];
   __shared__ uint16_t IA[2][64], IB[2][64];
   const int TB = si.T;
   const int rowsA = 1 << si.lm, rowsB = 1 << si.ln;
+  // Dynamic shared memory: A rows, B rows, leaf residual rows, row offsets.
   T* As = reinterpret_cast<T*>(sm_dyn);
   T* Bs = As + (size_t)rowsA * KK;
   float* Alo = reinterpret_cast<float*>(Bs + (size_t)rowsB * KK);
   float* Blo = Alo + (jd.a.ptr_lo ? (size_t)rowsA * KK : 0);
+  int32_t* offA = reinterpret_cast<int32_t*>(Blo + (jd.b.ptr_lo ? (size_t)rowsB * KK : 0));
+  int32_t* offB = offA + rowsA;
   const int mnb = jd.mb + jd.nb;
   const uint64_t nmask = (1ull << jd.nb) - 1;
   const uint64_t lowmask = (1ull << TB) - 1;
@@ -785,12 +787,13 @@ bool launch_staged(int mode, const JoinDesc& jd, const int64_t* s0, int nslices,
     if (lm + ln != T || lm < 2 || ln < 2) continue;
     size_t bytes = ((size_t)1 << lm) * K * es + ((size_t)1 << ln) * K * es;
     if (mode == 1) bytes += (jd.a.ptr_lo ? ((size_t)1 << lm) * K * 4 : 0) + (jd.b.ptr_lo ? ((size_t)1 << ln) * K * 4 : 0);
+    bytes += 4 * (((size_t)1 << lm) + ((size_t)1 << ln));  // row offsets
     if (bytes > 64 * 1024) continue;
     si.T = T;
     si.lm = lm;
     si.ln = ln;
     const int64_t tiles = (int64_t)nslices << (mnb - T);
-    const int grid = (int)(tiles < 152 * 4 ? tiles : 152 * 4);
+    const int grid = (int)(tiles < 152 * 8 ? tiles : 152 * 8);
 #define TOGB_STAGED(KK)                                                                                   \
     {                                                                                                     \
       if (mode == 0) {                                                                                    \
