@@ -125,6 +125,40 @@ def cpu_baseline(prog, max_seconds=12.0, min_slices=2):
                       "extrapolated to the full count" % (n, prog.num_slices, dt)}
 
 
+def batch_line(args, dev):
+    """The uneven 512-instance batch (weighted cubic vertex cover n in [30,160]
+    and random 3-CNF v in [40,52], each with its own plan and 1..2^8 slices) as
+    one CUDA graph per step: counts/s, executed TFLOP/s and the worst error
+    against the reference's counts recorded for 252 of the instances."""
+    import torch
+
+    from tensororder_gb300 import batch, runtime
+    from tensororder_gb300.run_batch import load
+
+    progs, refs, _ = load(os.path.join(ROOT, "tensororder_gb300", "plans", "batch512.json.gz"))
+    ex = batch.BatchExecutor(progs, runtime.MODE_SPLIT, device=dev.index or 0, nstreams=16)
+    stream = torch.cuda.current_stream(dev)
+    ex.run(stream)  # warm-up (graph upload)
+    torch.cuda.synchronize(dev)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(max(1, args.batch_steps)):
+        ex.run(stream)
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b) / max(1, args.batch_steps)
+    counts = ex.counts(stream)
+    work = ex.work()
+    ex.close()
+    have = ~np.isnan(refs)
+    rel = np.abs(counts[have] - refs[have]) / np.abs(refs[have])
+    return {"instances": len(progs), "slices": work["slices"], "ms_per_step": ms,
+            "counts_per_s": len(progs) * 1e3 / ms, "executed_tflops": work["executed_flops"] / (ms * 1e-3) / 1e12,
+            "max_rel_err_vs_reference": float(rel.max()), "checked": int(have.sum()), "steps": args.batch_steps,
+            "form": "split", "graph": "one CUDA graph per step, 16 internal streams"}
+
+
 def run_reference(args, rank, world):
     doc, prog = load_workload()
     if rank != 0:
@@ -166,6 +200,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--ref-sample", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-steps", type=int, default=2)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -339,6 +375,8 @@ def main():
         # per count: the slice-invariant joins, the slice base, the per-slice joins and the root
         "gpu_launches": (int(info.num_launches) + 1 + int(info.num_joins_once)) * args.steps,
     }
+    if not args.no_batch:
+        line["batch512"] = batch_line(args, dev)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(prog)
     if world > 1:
