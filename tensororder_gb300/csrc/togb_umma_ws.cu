@@ -93,7 +93,7 @@ struct TileMap {
 // The stage ring and the two accumulator sets run continuously across tiles,
 // so the next tile's loads, conversions and first MMAs overlap the current
 // tile's epilogue.
-template <int BN, int NR, int NC>
+template <int BN, int NR, int NC, bool PAIRS>
 __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant__ JoinDesc jd,
                                                           const __grid_constant__ CUtensorMap tmA,
                                                           const __grid_constant__ CUtensorMap tmB,
@@ -270,27 +270,57 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
       float acc[HALF];
 #pragma unroll
       for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
-      for (int w = 0; w < nwin; ++w, ++gw) {
-        const int set = gw % NSETS;
-        if (!mbar_wait_or_abort(smem_u32(&accf[set]), (gw / NSETS) & 1, abort)) {
-          *abort = 1;
-          break;
-        }
-        tc_fence_after();
-#pragma unroll
-        for (int col = 0; col < HALF; col += 32) {
-          float v0[16], v1[16];
-          tmem_ld16(tl + (uint32_t)(set * BN + col), v0);
-          tmem_ld16(tl + (uint32_t)(set * BN + col + 16), v1);
-          tmem_ld_wait();
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            acc[col + j] += v0[j];
-            acc[col + 16 + j] += v1[j];
+      if constexpr (PAIRS) {
+        // Long K: windows are read in pairs and added to each other before
+        // they are added into the running sum, halving the rounding steps of
+        // the long FP32 accumulation.
+        for (int w = 0; w < nwin;) {
+          const bool two = w + 1 < nwin;
+          const int set0 = gw % NSETS, set1 = (gw + 1) % NSETS;
+          if (!mbar_wait_or_abort(smem_u32(&accf[set0]), (gw / NSETS) & 1, abort) ||
+              (two && !mbar_wait_or_abort(smem_u32(&accf[set1]), ((gw + 1) / NSETS) & 1, abort))) {
+            *abort = 1;
+            break;
           }
+          tc_fence_after();
+#pragma unroll
+          for (int col = 0; col < HALF; col += 16) {
+            float v0[16], v1[16];
+            tmem_ld16(tl + (uint32_t)(set0 * BN + col), v0);
+            if (two) tmem_ld16(tl + (uint32_t)(set1 * BN + col), v1);
+            tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) acc[col + j] += two ? v0[j] + v1[j] : v0[j];
+          }
+          tc_fence_before();
+          mbar_arrive(smem_u32(&acce[set0]));
+          if (two) mbar_arrive(smem_u32(&acce[set1]));
+          w += two ? 2 : 1;
+          gw += two ? 2 : 1;
         }
-        tc_fence_before();
-        mbar_arrive(smem_u32(&acce[set]));
+      } else {
+        for (int w = 0; w < nwin; ++w, ++gw) {
+          const int set = gw % NSETS;
+          if (!mbar_wait_or_abort(smem_u32(&accf[set]), (gw / NSETS) & 1, abort)) {
+            *abort = 1;
+            break;
+          }
+          tc_fence_after();
+#pragma unroll
+          for (int col = 0; col < HALF; col += 32) {
+            float v0[16], v1[16];
+            tmem_ld16(tl + (uint32_t)(set * BN + col), v0);
+            tmem_ld16(tl + (uint32_t)(set * BN + col + 16), v1);
+            tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              acc[col + j] += v0[j];
+              acc[col + 16 + j] += v1[j];
+            }
+          }
+          tc_fence_before();
+          mbar_arrive(smem_u32(&acce[set]));
+        }
       }
       if (*abort) break;
       const int mlim = (int)min((int64_t)kBM, M - (int64_t)m0);
@@ -354,11 +384,11 @@ int sm_count() {
   return sms[dev];
 }
 
-template <int BN, int NR, int NC>
+template <int BN, int NR, int NC, bool PAIRS>
 cudaError_t launch_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorMap& tb, int nslices,
                       cudaStream_t st) {
   using L = WsSmem<BN, NR, NC>;
-  cudaError_t e = cudaFuncSetAttribute(k_umma_ws<BN, NR, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::DYN);
+  cudaError_t e = cudaFuncSetAttribute(k_umma_ws<BN, NR, NC, PAIRS>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::DYN);
   if (e != cudaSuccess) return e;
   constexpr int bn_bits = BN == 128 ? 7 : 6;
   TileMap tm;
@@ -368,7 +398,7 @@ cudaError_t launch_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorM
   if (tm.tps_bits > 40) return cudaErrorInvalidValue;
   const int64_t ntiles = (int64_t)nslices << tm.tps_bits;
   const int64_t grid = ntiles < sm_count() ? ntiles : sm_count();
-  k_umma_ws<BN, NR, NC><<<(unsigned)grid, kWsThreads, L::DYN, st>>>(jd, ta, tb, ntiles, tm);
+  k_umma_ws<BN, NR, NC, PAIRS><<<(unsigned)grid, kWsThreads, L::DYN, st>>>(jd, ta, tb, ntiles, tm);
   return cudaGetLastError();
 }
 
@@ -378,8 +408,11 @@ int umma_ws_box_rows_b(int nb) { return nb >= 7 ? 128 : 64; }
 
 cudaError_t launch_umma_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorMap& tb, int nslices,
                            cudaStream_t st) {
-  if (jd.nb >= 7) return launch_ws<128, 2, 2>(jd, ta, tb, nslices, st);
-  return launch_ws<64, 4, 2>(jd, ta, tb, nslices, st);
+  // More than 64 windows of 16 (K > 1024): the paired read-out.
+  const bool pairs = jd.kb > 10;
+  if (jd.nb >= 7)
+    return pairs ? launch_ws<128, 2, 2, true>(jd, ta, tb, nslices, st) : launch_ws<128, 2, 2, false>(jd, ta, tb, nslices, st);
+  return pairs ? launch_ws<64, 4, 2, true>(jd, ta, tb, nslices, st) : launch_ws<64, 4, 2, false>(jd, ta, tb, nslices, st);
 }
 
 }  // namespace togb
