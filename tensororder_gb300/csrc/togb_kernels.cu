@@ -146,6 +146,12 @@ __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ Joi
   const T* __restrict__ A = (const T*)jd.a.ptr;
   const T* __restrict__ B = (const T*)jd.b.ptr;
   T* __restrict__ C = (T*)jd.c_ptr;
+  // Split form: each lane group keeps the running maximum of its current slice
+  // across iterations and publishes it (one atomic per group) only when the
+  // slice changes, so a large single-slice output costs a few atomics per warp
+  // rather than one per iteration.  Every flush decision is warp-uniform.
+  uint32_t carry = 0;
+  int carry_b = -1;
   for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < groups_pad;
        g += (int64_t)gridDim.x * blockDim.x) {
     const bool valid = g < groups;
@@ -192,9 +198,23 @@ __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ Joi
       }
     }
     if (MODE == 1) {
-      for (int off = 1; off < lanes; off <<= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, off));
-      if (valid && (threadIdx.x & (lanes - 1)) == 0) atomicMax(&jd.c_max[b], bits);
+      if (__any_sync(0xffffffffu, valid && b != carry_b)) {
+        uint32_t v = carry;
+        for (int off = 1; off < lanes; off <<= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
+        if (carry_b >= 0 && (threadIdx.x & (lanes - 1)) == 0) atomicMax(&jd.c_max[carry_b], v);
+        carry = 0;
+        carry_b = -1;
+      }
+      if (valid) {
+        carry = max(carry, bits);
+        carry_b = b;
+      }
     }
+  }
+  if (MODE == 1) {
+    uint32_t v = carry;
+    for (int off = 1; off < lanes; off <<= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
+    if (carry_b >= 0 && (threadIdx.x & (lanes - 1)) == 0) atomicMax(&jd.c_max[carry_b], v);
   }
 }
 
