@@ -281,9 +281,20 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
   const int64_t tiles_per_slice = 1ll << (mnb - TB);
   const int64_t ntiles = (int64_t)nslices * tiles_per_slice;
   const int per_thread = (1 << TB) / (4 * kThreads);  // vector groups per thread (>= 1)
+  // Split form: the slice maximum is carried across this CTA's tiles and
+  // published (one atomic per warp) only when the slice changes.
+  uint32_t carry = 0;
+  int carry_b = -1;
   __syncthreads();
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int b = (int)(t / tiles_per_slice);
+    if (MODE == 1 && b != carry_b) {  // block-uniform
+      uint32_t v = carry;
+      for (int off = 16; off > 0; off >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
+      if (carry_b >= 0 && (threadIdx.x & 31) == 0) atomicMax(&jd.c_max[carry_b], v);
+      carry = 0;
+      carry_b = b;
+    }
     const uint64_t qh = (uint64_t)(t % tiles_per_slice) << TB;  // tile base address within the slice
     const int64_t s = s0 + b;
     const uint64_t mh = jd.c_natural ? (qh >> jd.nb) : (uint64_t)dep(jd.r_inv_m, qh);
@@ -349,10 +360,14 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
       store_vec(C + (int64_t)b * jd.c_batch_stride + qh + q0, out);
     }
     if (MODE == 1) {
-      for (int off = 16; off > 0; off >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, off));
-      if ((threadIdx.x & 31) == 0) atomicMax(&jd.c_max[b], bits);
+      carry = max(carry, bits);
       if (qh == 0 && threadIdx.x == 0) jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - sa - sb;
     }
+  }
+  if (MODE == 1) {
+    uint32_t v = carry;
+    for (int off = 16; off > 0; off >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
+    if (carry_b >= 0 && (threadIdx.x & 31) == 0) atomicMax(&jd.c_max[carry_b], v);
   }
 }
 
