@@ -332,7 +332,7 @@ def main():
         t1 = time.perf_counter()
         if i >= args.warmup:
             e2e_ms.append((t1 - t0) * 1e3)
-    h2d = int(sum((1 << l.rank) * 12 for l in prog.leaves))  # FP64 + FP32 leaf copies
+    h2d = int(dp.h2d_bytes)  # leaf parameters (clause/variable leaves are built on the device) + dense leaves
     d2h = 16 * (1 << int(info.root_rank))
 
     line = {

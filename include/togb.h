@@ -90,6 +90,33 @@ typedef struct {
 /* Lower and plan a program for `device`; copies the leaves to the device. */
 togb_status togb_program_create(const togb_program_desc* desc, int device, togb_program** out);
 
+/* Leaves of the two CNF tensor kinds described by their parameters, so the
+ * library builds their values on the device instead of receiving them:
+ *   TOGB_LEAF_CLAUSE    OrTensor.build (tensor_network_constructions.py:69-99):
+ *                       all ones except 0 at the all-false corner; with a
+ *                       factored gate output axis (output_index >= 0) the
+ *                       output axis's false value is 0 except at the
+ *                       all-false corner, whose output-flipped neighbour is 0;
+ *   TOGB_LEAF_VARIABLE  VariableTensor.build (:144-152): w_neg at all-zeros,
+ *                       w_pos at all-ones, 0 elsewhere (rank 0: w_neg + w_pos);
+ *   TOGB_LEAF_DENSE     values given in desc->leaf_values.
+ * `positive` has bit a set when axis a's literal is positive. */
+typedef enum { TOGB_LEAF_DENSE = 0, TOGB_LEAF_CLAUSE = 1, TOGB_LEAF_VARIABLE = 2 } togb_leaf_kind;
+typedef struct {
+  int32_t kind;
+  int32_t output_index;
+  uint32_t positive;
+  int32_t pad_;
+  double w_neg, w_pos;
+} togb_leaf_spec;
+
+/* togb_program_create with compact leaves: specs[i] describes leaf i;
+ * desc->leaf_values holds only the dense leaves' values, concatenated in leaf
+ * order (may be NULL when no leaf is dense).  Clause and variable leaves are
+ * materialised by a kernel on `device`. */
+togb_status togb_program_create_compact(const togb_program_desc* desc, const togb_leaf_spec* specs, int device,
+                                        togb_program** out);
+
 togb_status togb_program_info_get(const togb_program* prog, togb_program_info* info);
 
 /* Lower and plan a program on the host only (no device, no leaf values

@@ -104,7 +104,7 @@ class BatchExecutor:
 
     @property
     def h2d_bytes(self) -> int:
-        return int(sum(dp._values.nbytes * 1.5 for dp in self.dps))
+        return int(sum(dp.h2d_bytes for dp in self.dps))
 
     def run(self, stream=None):
         runtime.check(runtime.lib().togb_batch_run(self._h, runtime._stream_handle(stream)))

@@ -103,6 +103,18 @@ cudaError_t launch_umma_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUte
 // Rows of the B-operand TMA box of launch_umma_ws for an N of 2^nb.
 int umma_ws_box_rows_b(int nb);
 cudaError_t launch_set_s0(int64_t* d_s0, int64_t value, cudaStream_t st);
+// One leaf to materialise on the device (togb_program_create_compact).
+struct LeafBuild {
+  int64_t off;         // element offset of the leaf in the leaf arrays
+  int32_t rank;
+  int32_t kind;        // togb_leaf_kind
+  int32_t out_pos;     // clause: index bit of the gate output axis, -1 if none
+  uint32_t false_idx;  // clause: index of the all-false corner
+  double w_neg, w_pos; // variable weights
+};
+// Fill the FP64 values and the FP32 hi/lo split of every listed leaf.
+cudaError_t launch_build_leaves(const LeafBuild* items, int n, double* v64, float* v32, float* v32lo,
+                                cudaStream_t st);
 // out[e] = acc[e] + acc[E + e]: the compensated sum of a root accumulator.
 cudaError_t launch_finalize(const double* acc, int64_t E, double* out, cudaStream_t st);
 cudaError_t probe_peak(int kind, cudaStream_t st, double* flops);

@@ -741,6 +741,35 @@ __global__ void k_root(const __grid_constant__ RootDesc rd, const int64_t* __res
 
 __global__ void k_set_s0(int64_t* p, int64_t v) { *p = v; }
 
+// One CTA per leaf: the values of OrTensor / VariableTensor leaves from their
+// parameters (index bit R-1-a is axis a, row-major like the host layout).
+__global__ void k_build_leaves(const LeafBuild* __restrict__ items, double* __restrict__ v64,
+                               float* __restrict__ v32, float* __restrict__ v32lo) {
+  const LeafBuild it = items[blockIdx.x];
+  const uint64_t n = 1ull << it.rank;
+  const uint64_t all = n - 1;
+  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    double v;
+    if (it.kind == TOGB_LEAF_VARIABLE) {
+      v = it.rank == 0 ? it.w_neg + it.w_pos : (i == 0 ? it.w_neg : (i == all ? it.w_pos : 0.0));
+    } else {
+      const uint64_t F = it.false_idx;
+      if (it.out_pos < 0) {
+        v = i == F ? 0.0 : 1.0;
+      } else {
+        const uint64_t bo = 1ull << it.out_pos;
+        if (i == F) v = 1.0;
+        else if (i == (F ^ bo)) v = 0.0;
+        else v = ((i ^ F) & bo) ? 1.0 : 0.0;  // the output axis at its false value gives 0
+      }
+    }
+    const float hi = (float)v;
+    v64[it.off + i] = v;
+    v32[it.off + i] = hi;
+    v32lo[it.off + i] = (float)(v - (double)hi);
+  }
+}
+
 __global__ void k_finalize(const double* __restrict__ acc, int64_t E, double* __restrict__ out) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x)
     out[e] = acc[e] + acc[E + e];
@@ -914,6 +943,13 @@ cudaError_t launch_root(int mode, const RootDesc& rd, const int64_t* s0, int nsl
   const int g = grid_for(1ll << rd.r.outer_bits);
   if (mode == 0) k_root<0, double><<<g, kThreads, 0, st>>>(rd, s0, nslices);
   else k_root<1, float><<<g, kThreads, 0, st>>>(rd, s0, nslices);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_leaves(const LeafBuild* items, int n, double* v64, float* v32, float* v32lo,
+                                cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_build_leaves<<<n, kThreads, 0, st>>>(items, v64, v32, v32lo);
   return cudaGetLastError();
 }
 

@@ -707,7 +707,8 @@ namespace {
 
 // Host half of togb_program_create: validation, lowering and planning.  No
 // device memory is touched.  Leaf values are validated only when present.
-togb_status lower_host(const togb_program_desc* d, int device, togb_program** out, int64_t* num_values) {
+togb_status lower_host(const togb_program_desc* d, int device, togb_program** out, int64_t* num_values,
+                       const togb_leaf_spec* specs = nullptr) {
   if (!d || !out) return fail(TOGB_ERR_INVALID, "null argument");
   *out = nullptr;
   if (d->num_leaves <= 0 || d->num_tokens <= 0) return fail(TOGB_ERR_INVALID, "empty program");
@@ -733,7 +734,7 @@ togb_status lower_host(const togb_program_desc* d, int device, togb_program** ou
   p->leaf_axes.resize(d->num_leaves);
   p->leaf_off.resize(d->num_leaves);
   p->leaf_shift.resize(d->num_leaves);
-  int64_t ax = 0, voff = 0;
+  int64_t ax = 0, voff = 0, dense_off = 0;
   for (int l = 0; l < d->num_leaves; ++l) {
     const int r = d->leaf_rank[l];
     if (r < 0 || r > 30) { delete p; return fail(TOGB_ERR_UNSUPPORTED, "leaf rank outside [0, 30]"); }
@@ -741,13 +742,32 @@ togb_status lower_host(const togb_program_desc* d, int device, togb_program** ou
     ax += r;
     p->leaf_off[l] = voff;
     double mx = 0;
-    for (int64_t i = 0; d->leaf_values && i < pow2(r); ++i) {
-      const double v = d->leaf_values[voff + i];
-      if (!(v >= 0) || std::isinf(v)) {
+    const int kind = specs ? specs[l].kind : TOGB_LEAF_DENSE;
+    if (kind == TOGB_LEAF_VARIABLE) {
+      const double wn = specs[l].w_neg, wp = specs[l].w_pos;
+      if (!(wn >= 0) || !(wp >= 0) || std::isinf(wn) || std::isinf(wp)) {
         delete p;
-        return fail(TOGB_ERR_UNSUPPORTED, "leaf entries must be finite and non-negative");
+        return fail(TOGB_ERR_UNSUPPORTED, "variable weights must be finite and non-negative");
       }
-      mx = std::max(mx, v);
+      mx = r == 0 ? wn + wp : std::max(wn, wp);
+    } else if (kind == TOGB_LEAF_CLAUSE) {
+      if (specs[l].output_index >= r) { delete p; return fail(TOGB_ERR_INVALID, "clause output axis out of range"); }
+      mx = 1.0;
+    } else if (kind == TOGB_LEAF_DENSE) {
+      const double* vals = d->leaf_values ? d->leaf_values + (specs ? dense_off : voff) : nullptr;
+      if (specs && !vals) { delete p; return fail(TOGB_ERR_INVALID, "dense leaf without values"); }
+      for (int64_t i = 0; vals && i < pow2(r); ++i) {
+        const double v = vals[i];
+        if (!(v >= 0) || std::isinf(v)) {
+          delete p;
+          return fail(TOGB_ERR_UNSUPPORTED, "leaf entries must be finite and non-negative");
+        }
+        mx = std::max(mx, v);
+      }
+      dense_off += pow2(r);
+    } else {
+      delete p;
+      return fail(TOGB_ERR_INVALID, "unknown leaf kind");
     }
     int e2 = 0;
     if (mx > 0) std::frexp(mx, &e2);  // mx in [2^(e2-1), 2^e2)
@@ -845,6 +865,79 @@ togb_status togb_program_create(const togb_program_desc* d, int device, togb_pro
       (e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking)) != cudaSuccess) {
     togb_program_destroy(p);
     return cuda_fail(e, "program allocation");
+  }
+  *out = p;
+  return TOGB_OK;
+}
+
+togb_status togb_program_create_compact(const togb_program_desc* d, const togb_leaf_spec* specs, int device,
+                                        togb_program** out) {
+  if (!d || !out || !specs) return fail(TOGB_ERR_INVALID, "null argument");
+  *out = nullptr;
+  togb_program* p = nullptr;
+  int64_t voff = 0;
+  togb_status st = lower_host(d, device, &p, &voff, specs);
+  if (st != TOGB_OK) return st;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) { delete p; return cuda_fail(e, "cudaSetDevice"); }
+  const int64_t E = pow2(p->nodes[p->root].rank);
+  std::vector<togb::LeafBuild> items;
+  for (int l = 0; l < d->num_leaves; ++l) {
+    if (specs[l].kind == TOGB_LEAF_DENSE) continue;
+    togb::LeafBuild it{};
+    const int r = p->leaf_rank[l];
+    it.off = p->leaf_off[l];
+    it.rank = r;
+    it.kind = specs[l].kind;
+    it.out_pos = specs[l].output_index >= 0 ? r - 1 - specs[l].output_index : -1;
+    for (int a = 0; a < r; ++a)
+      if (!((specs[l].positive >> a) & 1)) it.false_idx |= 1u << (r - 1 - a);
+    it.w_neg = specs[l].w_neg;
+    it.w_pos = specs[l].w_pos;
+    items.push_back(it);
+  }
+  togb::LeafBuild* d_items = nullptr;
+  if ((e = cudaMalloc(&p->d_leaf64, std::max<int64_t>(voff, 1) * 8)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_leaf32, std::max<int64_t>(voff, 1) * 4)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_leaf32lo, std::max<int64_t>(voff, 1) * 4)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_acc, 2 * E * 8)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_s0, 8)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_err, 4)) != cudaSuccess ||
+      (e = cudaMemset(p->d_err, 0, 4)) != cudaSuccess ||
+      (e = cudaMemset(p->d_acc, 0, 2 * E * 8)) != cudaSuccess ||
+      (e = cudaMemset(p->d_s0, 0, 8)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (!items.empty() && (e = cudaMalloc(&d_items, items.size() * sizeof(togb::LeafBuild))) != cudaSuccess)) {
+    togb_program_destroy(p);
+    return cuda_fail(e, "program allocation");
+  }
+  // Dense leaves: their values, and the FP32 split, copied leaf by leaf.
+  int64_t dense_off = 0;
+  for (int l = 0; e == cudaSuccess && l < d->num_leaves; ++l) {
+    if (specs[l].kind != TOGB_LEAF_DENSE) continue;
+    const int64_t n = pow2(p->leaf_rank[l]);
+    const double* v = d->leaf_values + dense_off;
+    std::vector<float> hi(n), lo(n);
+    for (int64_t i = 0; i < n; ++i) {
+      hi[i] = (float)v[i];
+      lo[i] = (float)(v[i] - (double)hi[i]);
+    }
+    const int64_t o = p->leaf_off[l];
+    if ((e = cudaMemcpy(p->d_leaf64 + o, v, n * 8, cudaMemcpyHostToDevice)) == cudaSuccess &&
+        (e = cudaMemcpy(p->d_leaf32 + o, hi.data(), n * 4, cudaMemcpyHostToDevice)) == cudaSuccess)
+      e = cudaMemcpy(p->d_leaf32lo + o, lo.data(), n * 4, cudaMemcpyHostToDevice);
+    dense_off += n;
+  }
+  if (e == cudaSuccess && !items.empty() &&
+      (e = cudaMemcpy(d_items, items.data(), items.size() * sizeof(togb::LeafBuild), cudaMemcpyHostToDevice)) ==
+          cudaSuccess &&
+      (e = togb::launch_build_leaves(d_items, (int)items.size(), p->d_leaf64, p->d_leaf32, p->d_leaf32lo, nullptr)) ==
+          cudaSuccess)
+    e = cudaDeviceSynchronize();
+  if (d_items) cudaFree(d_items);
+  if (e != cudaSuccess) {
+    togb_program_destroy(p);
+    return cuda_fail(e, "leaf build");
   }
   *out = p;
   return TOGB_OK;

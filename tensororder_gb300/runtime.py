@@ -55,6 +55,22 @@ class ProgramInfo(ctypes.Structure):
     ]
 
 
+class LeafSpec(ctypes.Structure):
+    """togb_leaf_spec: a clause or variable leaf by its parameters."""
+
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("output_index", ctypes.c_int32),
+        ("positive", ctypes.c_uint32),
+        ("pad_", ctypes.c_int32),
+        ("w_neg", ctypes.c_double),
+        ("w_pos", ctypes.c_double),
+    ]
+
+
+LEAF_DENSE, LEAF_CLAUSE, LEAF_VARIABLE = 0, 1, 2
+
+
 class TogbError(RuntimeError):
     """A failed call into libtogb; ``status`` is the togb_status code."""
 
@@ -76,7 +92,7 @@ EXPORTS = [
     "togb_contract_static_f64", "togb_program_joins", "togb_program_set_kernel", "togb_program_kernel_allowed",
     "togb_mlp_param_count", "togb_mlp_scratch_floats", "togb_mlp_forward", "togb_mlp_loss_grad", "togb_mlp_adam",
     "togb_batch_create", "togb_batch_run", "togb_batch_results", "togb_batch_destroy",
-    "togb_program_create_host", "togb_program_describe",
+    "togb_program_create_host", "togb_program_describe", "togb_program_create_compact",
 ]
 
 KERNEL_NAMES = {0: "direct", 1: "tiled", 2: "reduce", 3: "tensor"}
@@ -120,6 +136,8 @@ def lib():
                                     ctypes.POINTER(ctypes.c_size_t), ctypes.c_int32, ctypes.POINTER(c_void)]
     L.togb_batch_run.argtypes = [c_void, c_void]
     L.togb_program_create_host.argtypes = [ctypes.POINTER(ProgramDesc), ctypes.POINTER(c_void)]
+    L.togb_program_create_compact.argtypes = [ctypes.POINTER(ProgramDesc), ctypes.POINTER(LeafSpec), ctypes.c_int,
+                                              ctypes.POINTER(c_void)]
     L.togb_program_describe.argtypes = [c_void, ctypes.c_int, ctypes.c_int32, ctypes.c_char_p, ctypes.c_size_t]
     L.togb_batch_results.argtypes = [c_void, c_void, _f64p, ctypes.c_int32]
     L.togb_batch_destroy.argtypes = [c_void]
@@ -149,15 +167,36 @@ def _stream_handle(stream):
 
 
 class _Desc:
-    """A togb_program_desc with the arrays it points into kept alive."""
+    """A togb_program_desc with the arrays it points into kept alive.
 
-    def __init__(self, program: Program, with_values=True):
+    ``values``: "all" concatenates every leaf's dense values (togb_program_create),
+    "dense" only the dense leaves' (togb_program_create_compact, with ``specs``
+    describing the clause and variable leaves), None none at all."""
+
+    def __init__(self, program: Program, values="all"):
         leaves = program.leaves
         self.ranks = np.array([l.rank for l in leaves], dtype=np.int32)
         self.axes = np.array([a for l in leaves for a in l.axes] or [0], dtype=np.int32)
-        if with_values:
+        self.specs = None
+        if values == "all":
             vals = [l.parent().ravel() for l in leaves]
             self.values = np.ascontiguousarray(np.concatenate(vals) if vals else np.zeros(1), dtype=np.float64)
+        elif values == "dense":
+            specs = (LeafSpec * max(1, len(leaves)))()
+            vals = []
+            for i, l in enumerate(leaves):
+                if l.kind == "or" and l.rank <= 30:
+                    specs[i].kind = LEAF_CLAUSE
+                    specs[i].output_index = -1 if l.output_index is None else int(l.output_index)
+                    specs[i].positive = sum(1 << a for a, pos in enumerate(l.positive) if pos)
+                elif l.kind == "var":
+                    specs[i].kind = LEAF_VARIABLE
+                    specs[i].w_neg, specs[i].w_pos = float(l.w_neg), float(l.w_pos)
+                else:
+                    specs[i].kind = LEAF_DENSE
+                    vals.append(l.parent().ravel())
+            self.specs = specs
+            self.values = np.ascontiguousarray(np.concatenate(vals), dtype=np.float64) if vals else None
         else:
             self.values = None
         self.tokens = np.array(program.postorder, dtype=np.int32)
@@ -176,7 +215,7 @@ class HostProgram:
 
     def __init__(self, program: Program):
         self.program = program
-        self._d = _Desc(program, with_values=False)
+        self._d = _Desc(program, values=None)
         handle = ctypes.c_void_p()
         check(lib().togb_program_create_host(ctypes.byref(self._d.desc), ctypes.byref(handle)))
         self._h = handle
@@ -215,18 +254,38 @@ class HostProgram:
 class DeviceProgram:
     """A program lowered and planned by libtogb, with its leaves on the device."""
 
-    def __init__(self, program: Program, device: int = 0):
+    def __init__(self, program: Program, device: int = 0, leaves: str = "device"):
+        """``leaves="device"``: clause and variable leaves are described by
+        their parameters and built on the device, only dense leaves' values are
+        uploaded (togb_program_create_compact).  ``leaves="host"``: every
+        leaf's dense values are built here and uploaded (togb_program_create)."""
         self.program = program
         self.device = device
-        self._d = _Desc(program)
-        self._values = self._d.values
         handle = ctypes.c_void_p()
-        check(lib().togb_program_create(ctypes.byref(self._d.desc), device, ctypes.byref(handle)))
+        if leaves == "device":
+            self._d = _Desc(program, values="dense")
+            self.h2d_bytes = (0 if self._d.values is None else self._d.values.nbytes * 2) + \
+                ctypes.sizeof(LeafSpec) * len(program.leaves)
+            check(lib().togb_program_create_compact(ctypes.byref(self._d.desc), self._d.specs, device,
+                                                    ctypes.byref(handle)))
+        elif leaves == "host":
+            self._d = _Desc(program, values="all")
+            self.h2d_bytes = self._d.values.nbytes * 2
+            check(lib().togb_program_create(ctypes.byref(self._d.desc), device, ctypes.byref(handle)))
+        else:
+            raise ValueError("leaves must be 'device' or 'host'")
         self._h = handle
         info = ProgramInfo()
         check(lib().togb_program_info_get(self._h, ctypes.byref(info)))
         self.info = info
         self._workspace = None
+
+    @property
+    def _values(self):
+        """Every leaf's dense values concatenated (the layout the leaf arrays
+        have on the device), built on the host on demand."""
+        vals = [l.parent().ravel() for l in self.program.leaves]
+        return np.ascontiguousarray(np.concatenate(vals) if vals else np.zeros(1), dtype=np.float64)
 
     @property
     def num_slices(self):

@@ -128,3 +128,20 @@ def test_weighted_cubic_vc_220_sliced_1024(mode, tol, cuda):
     prog = Program.from_dict(doc["program"])
     got = float(api.GB300API(mode=mode).contract_program(prog))
     assert rel(got, doc["reference"]["float64"]) <= tol
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("mode", [runtime.MODE_F64, runtime.MODE_SPLIT])
+def test_leaves_built_on_device_match_uploaded_leaves(name, mode, cuda):
+    """Clause and variable leaves built by the library from their parameters
+    (togb_program_create_compact) give exactly the count of the same program
+    with every leaf's dense values uploaded (togb_program_create)."""
+    prog = program(name)
+    got = []
+    for leaves in ("device", "host"):
+        dp = runtime.DeviceProgram(prog, leaves=leaves)
+        dp.reset()
+        dp.run(mode)
+        got.append(dp.result().copy())
+        dp.close()
+    assert np.array_equal(got[0], got[1])

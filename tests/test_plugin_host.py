@@ -83,3 +83,37 @@ def test_oom_maps_to_reference_error(monkeypatch):
     prog = Program.from_dict(load_golden("wvc18_s2")["program"])
     with pytest.raises(api._OOM):
         api.GB300API().contract_program(prog)
+
+
+def _device_leaf_formula(spec, rank):
+    """The value rule of the library's leaf-building kernel (k_build_leaves),
+    restated on the host from a togb_leaf_spec."""
+    n = 1 << rank
+    out = np.zeros(n)
+    if spec.kind == runtime.LEAF_VARIABLE:
+        if rank == 0:
+            return np.array(spec.w_neg + spec.w_pos)
+        out[0], out[n - 1] = spec.w_neg, spec.w_pos
+        return out.reshape((2,) * rank)
+    F = sum(1 << (rank - 1 - a) for a in range(rank) if not (spec.positive >> a) & 1)
+    for i in range(n):
+        if spec.output_index < 0:
+            out[i] = 0.0 if i == F else 1.0
+        else:
+            bo = 1 << (rank - 1 - spec.output_index)
+            out[i] = 1.0 if i == F else (0.0 if i == (F ^ bo) else (1.0 if (i ^ F) & bo else 0.0))
+    return out.reshape((2,) * rank)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_leaf_specs_describe_the_reference_leaves(name):
+    """Every clause and variable leaf, encoded as togb_leaf_spec, expands by the
+    device kernel's rule to the values OrTensor/VariableTensor.build give."""
+    prog = Program.from_dict(load_golden(name)["program"])
+    d = runtime._Desc(prog, values="dense")
+    for i, leaf in enumerate(prog.leaves):
+        spec = d.specs[i]
+        if spec.kind == runtime.LEAF_DENSE:
+            assert leaf.kind == "dense"
+            continue
+        assert np.array_equal(_device_leaf_formula(spec, leaf.rank), leaf.parent())
