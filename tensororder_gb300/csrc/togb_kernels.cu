@@ -222,14 +222,45 @@ __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ Joi
 // Each CTA takes tiles of 2^T consecutive output addresses of one slice.  The
 // T lowest address bits belong to lm bits of m and ln bits of n (lm + ln = T),
 // so a tile reads just 2^lm rows of A and 2^ln rows of B: the CTA loads those
-// rows (K values each) into shared memory once, then every thread computes
-// four consecutive outputs from shared memory and stores them as one vector.
+// rows (K values each) into shared memory, then every thread computes four
+// consecutive outputs from shared memory and stores them as one vector.
 // Output addresses are dense per slice, so a tile is one contiguous run.
+// When one operand does not vary with the slice, every CTA walks a contiguous
+// range of tiles with the slice index fastest and keeps that operand's rows
+// staged while the tile position stays the same: only the other operand's
+// rows are loaded again for each slice.
 struct StageInfo {
   int T, lm, ln;
+  int slice_fast;       // tiles ordered slice-fastest in contiguous CTA ranges
+  int a_inv, b_inv;     // the operand is the same for every slice
   int a_row_bits[12];   // A s_outer index of the r-th staged m bit
   int b_row_bits[12];
 };
+
+// One staged row of KK values from shared memory, in 16-byte (or 8-byte)
+// pieces where the row size allows.
+template <class T, int KK>
+__device__ __forceinline__ void lds_row(const T* __restrict__ p, T* v) {
+  constexpr int BYTES = KK * (int)sizeof(T);
+  if constexpr (BYTES % 16 == 0) {
+#pragma unroll
+    for (int c = 0; c < BYTES / 16; ++c) {
+      if constexpr (sizeof(T) == 4) {
+        const float4 x = reinterpret_cast<const float4*>(p)[c];
+        v[4 * c] = x.x; v[4 * c + 1] = x.y; v[4 * c + 2] = x.z; v[4 * c + 3] = x.w;
+      } else {
+        const double2 x = reinterpret_cast<const double2*>(p)[c];
+        v[2 * c] = x.x; v[2 * c + 1] = x.y;
+      }
+    }
+  } else if constexpr (BYTES == 8 && sizeof(T) == 4) {
+    const float2 x = reinterpret_cast<const float2*>(p)[0];
+    v[0] = x.x; v[1] = x.y;
+  } else {
+#pragma unroll
+    for (int k = 0; k < KK; ++k) v[k] = p[k];
+  }
+}
 
 template <int MODE, class T, int KK>
 __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constant__ JoinDesc jd,
@@ -274,20 +305,41 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
       if ((r >> b) & 1) o += jd.b.s_outer[si.b_row_bits[b]];
     offB[r] = (int32_t)o;
   }
+  __syncthreads();
   const T* __restrict__ A = (const T*)jd.a.ptr;
   const T* __restrict__ B = (const T*)jd.b.ptr;
   T* __restrict__ C = (T*)jd.c_ptr;
   const int64_t s0 = d_s0 ? *d_s0 : 0;
   const int64_t tiles_per_slice = 1ll << (mnb - TB);
   const int64_t ntiles = (int64_t)nslices * tiles_per_slice;
-  const int per_thread = (1 << TB) / (4 * kThreads);  // vector groups per thread (>= 1)
+  const int per_thread = (1 << TB) / (4 * kThreads);  // vector groups per thread: 1, 2 or 4
+  int64_t t_begin, t_end, t_step;
+  if (si.slice_fast) {
+    const int64_t chunk = (ntiles + gridDim.x - 1) / gridDim.x;
+    t_begin = (int64_t)blockIdx.x * chunk;
+    t_end = min(ntiles, t_begin + chunk);
+    t_step = 1;
+  } else {
+    t_begin = blockIdx.x;
+    t_end = ntiles;
+    t_step = gridDim.x;
+  }
   // Split form: the slice maximum is carried across this CTA's tiles and
   // published (one atomic per warp) only when the slice changes.
   uint32_t carry = 0;
   int carry_b = -1;
-  __syncthreads();
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int b = (int)(t / tiles_per_slice);
+  int64_t staged_pos = -1;  // tile position whose rows are staged
+  int staged_b = -1;        // slice whose rows are staged
+  for (int64_t t = t_begin; t < t_end; t += t_step) {
+    int b;
+    int64_t pos;
+    if (si.slice_fast) {
+      pos = t / nslices;
+      b = (int)(t - pos * nslices);
+    } else {
+      b = (int)(t / tiles_per_slice);
+      pos = t - (int64_t)b * tiles_per_slice;
+    }
     if (MODE == 1 && b != carry_b) {  // block-uniform
       uint32_t v = carry;
       for (int off = 16; off > 0; off >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
@@ -295,12 +347,8 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
       carry = 0;
       carry_b = b;
     }
-    const uint64_t qh = (uint64_t)(t % tiles_per_slice) << TB;  // tile base address within the slice
+    const uint64_t qh = (uint64_t)pos << TB;  // tile base address within the slice
     const int64_t s = s0 + b;
-    const uint64_t mh = jd.c_natural ? (qh >> jd.nb) : (uint64_t)dep(jd.r_inv_m, qh);
-    const uint64_t nh = jd.c_natural ? (qh & nmask) : (uint64_t)dep(jd.r_inv_n, qh);
-    const int64_t baseA = slice_offset(jd.a, b, s) + dep(jd.a.r_outer, mh);
-    const int64_t baseB = slice_offset(jd.b, b, s) + dep(jd.b.r_outer, nh);
     int sa = 0, sb = 0;
     float fa = 1.f, fb = 1.f;
     if (MODE == 1) {
@@ -309,21 +357,36 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
       fa = pow2f(sa);
       fb = pow2f(sb);
     }
-    __syncthreads();  // the previous tile's reads of the staged rows are done
-    for (int e = threadIdx.x; e < rowsA * KK; e += blockDim.x) {
-      const int r = e / KK, k = e - r * KK;
-      const int64_t o = baseA + offA[r] + jd.a.ktab[k];
-      As[e] = A[o];
-      if (MODE == 1 && jd.a.ptr_lo) Alo[e] = ((const float*)jd.a.ptr_lo)[o];
+    const bool newA = pos != staged_pos || (!si.a_inv && b != staged_b);
+    const bool newB = pos != staged_pos || (!si.b_inv && b != staged_b);
+    if (newA || newB) {  // block-uniform
+      const uint64_t mh = jd.c_natural ? (qh >> jd.nb) : (uint64_t)dep(jd.r_inv_m, qh);
+      const uint64_t nh = jd.c_natural ? (qh & nmask) : (uint64_t)dep(jd.r_inv_n, qh);
+      __syncthreads();  // the previous tile's reads of the staged rows are done
+      if (newA) {
+        const int64_t baseA = slice_offset(jd.a, b, s) + dep(jd.a.r_outer, mh);
+        for (int e = threadIdx.x; e < rowsA * KK; e += blockDim.x) {
+          const int r = e / KK, k = e - r * KK;
+          const int64_t o = baseA + offA[r] + jd.a.ktab[k];
+          As[e] = A[o];
+          if (MODE == 1 && jd.a.ptr_lo) Alo[e] = ((const float*)jd.a.ptr_lo)[o];
+        }
+      }
+      if (newB) {
+        const int64_t baseB = slice_offset(jd.b, b, s) + dep(jd.b.r_outer, nh);
+        for (int e = threadIdx.x; e < rowsB * KK; e += blockDim.x) {
+          const int r = e / KK, k = e - r * KK;
+          const int64_t o = baseB + offB[r] + jd.b.ktab[k];
+          Bs[e] = B[o];
+          if (MODE == 1 && jd.b.ptr_lo) Blo[e] = ((const float*)jd.b.ptr_lo)[o];
+        }
+      }
+      staged_pos = pos;
+      staged_b = b;
+      __syncthreads();
     }
-    for (int e = threadIdx.x; e < rowsB * KK; e += blockDim.x) {
-      const int r = e / KK, k = e - r * KK;
-      const int64_t o = baseB + offB[r] + jd.b.ktab[k];
-      Bs[e] = B[o];
-      if (MODE == 1 && jd.b.ptr_lo) Blo[e] = ((const float*)jd.b.ptr_lo)[o];
-    }
-    __syncthreads();
     uint32_t bits = 0;
+#pragma unroll 1
     for (int i = 0; i < per_thread; ++i) {
       const int q0 = 4 * (threadIdx.x + kThreads * i);
       T out[4];
@@ -332,17 +395,20 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
         const int q = q0 + j;
         const int ra = IA[0][q & 63] | IA[1][(q >> 6) & 63];
         const int rb = IB[0][q & 63] | IB[1][(q >> 6) & 63];
-        const T* ar = As + ra * KK;
-        const T* br = Bs + rb * KK;
+        T ar[KK], br[KK];
+        lds_row<T, KK>(As + ra * KK, ar);
+        lds_row<T, KK>(Bs + rb * KK, br);
         if (MODE == 1) {
           float f = 0.f;
           if (jd.a.ptr_lo) {
-            const float* al = Alo + ra * KK;
+            float al[KK];
+            lds_row<float, KK>(Alo + ra * KK, al);
 #pragma unroll
             for (int k = 0; k < KK; ++k) f = fmaf(al[k] * fa, (float)br[k] * fb, f);
           }
           if (jd.b.ptr_lo) {
-            const float* bl = Blo + rb * KK;
+            float bl[KK];
+            lds_row<float, KK>(Blo + rb * KK, bl);
 #pragma unroll
             for (int k = 0; k < KK; ++k) f = fmaf((float)ar[k] * fa, bl[k] * fb, f);
           }
@@ -369,6 +435,122 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
     for (int off = 16; off > 0; off >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
     if (carry_b >= 0 && (threadIdx.x & 31) == 0) atomicMax(&jd.c_max[carry_b], v);
   }
+}
+
+// Streaming variant for joins of a long operand A with a tiny B (N*K <= 16,
+// split form, A without a leaf residual): C[m][n] = sum_k A[m][k] * B[n][k]
+// with C row-major (natural).  A's two lowest m bits are either its two lowest
+// address bits (KFAST false: each k gives one 16-byte vector of four
+// consecutive m) or lie directly above all of its k bits (KFAST true: four
+// consecutive m and every k form one run of 4*K values).  Each thread takes
+// four consecutive m of one slice: it reads A as K vectors, keeps the slice's
+// B (and its residual) in registers, and writes its 4*N outputs, which are
+// contiguous, as N vectors.  The arithmetic order per output is dot_k's, so
+// the results equal k_direct's bit for bit.
+template <int KK, int NN, bool KFAST>
+__global__ void __launch_bounds__(kThreads) k_stream(const __grid_constant__ JoinDesc jd,
+                                                     const int64_t* __restrict__ d_s0, int nslices) {
+  const int qb = jd.mb - 2;  // log2 of the quads of m per slice
+  const int64_t quads = (int64_t)nslices << qb;
+  const int64_t quads_pad = (quads + 31) & ~(int64_t)31;
+  const int lanes = qb >= 5 ? 32 : (1 << qb);
+  const int mnb = jd.mb + jd.nb;
+  const int64_t s0 = d_s0 ? *d_s0 : 0;
+  const float* __restrict__ A = (const float*)jd.a.ptr;
+  const float* __restrict__ B = (const float*)jd.b.ptr;
+  const float* __restrict__ Blo = (const float*)jd.b.ptr_lo;
+  float* __restrict__ C = (float*)jd.c_ptr;
+  // Per-slice state, reloaded when a thread's slice changes.
+  int cur = -1, sa = 0, sb = 0;
+  float fa = 1.f;
+  int64_t abase = 0;
+  float bv[KK][NN], bl[KK][NN];
+  uint32_t carry = 0;
+  int carry_b = -1;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < quads_pad;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const bool valid = g < quads;
+    const int b = valid ? (int)(g >> qb) : 0;
+    uint32_t bits = 0;
+    if (valid) {
+      if (b != cur) {
+        cur = b;
+        const int64_t s = s0 + b;
+        sa = op_shift(jd.a, b);
+        sb = op_shift(jd.b, b);
+        fa = pow2f(sa);
+        const float fb = pow2f(sb);
+        abase = slice_offset(jd.a, b, s);
+        const int64_t bbase = slice_offset(jd.b, b, s);
+#pragma unroll
+        for (int n = 0; n < NN; ++n) {
+          const int64_t o = bbase + dep(jd.b.r_outer, (uint64_t)n);
+#pragma unroll
+          for (int k = 0; k < KK; ++k) {
+            bv[k][n] = B[o + jd.b.ktab[k]] * fb;
+            bl[k][n] = Blo ? Blo[o + jd.b.ktab[k]] * fb : 0.f;
+          }
+        }
+      }
+      const uint64_t m0 = ((uint64_t)g & ((1ull << qb) - 1)) << 2;
+      const int64_t ao = abase + dep(jd.a.r_outer, m0);
+      float av[4][KK];
+      if constexpr (KFAST) {
+        float x[4 * KK];
+#pragma unroll
+        for (int v = 0; v < KK; ++v) {
+          const float4 t = *reinterpret_cast<const float4*>(A + ao + 4 * v);
+          x[4 * v] = t.x; x[4 * v + 1] = t.y; x[4 * v + 2] = t.z; x[4 * v + 3] = t.w;
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int k = 0; k < KK; ++k) av[i][k] = x[i * KK + k] * fa;
+      } else {
+#pragma unroll
+        for (int k = 0; k < KK; ++k) {
+          const float4 t = *reinterpret_cast<const float4*>(A + ao + jd.a.ktab[k]);
+          av[0][k] = t.x * fa; av[1][k] = t.y * fa; av[2][k] = t.z * fa; av[3][k] = t.w * fa;
+        }
+      }
+      float out[4 * NN];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int n = 0; n < NN; ++n) {
+          float f = 0.f;
+          if (Blo) {
+#pragma unroll
+            for (int k = 0; k < KK; ++k) f = fmaf(av[i][k], bl[k][n], f);
+          }
+#pragma unroll
+          for (int k = 0; k < KK; ++k) f = fmaf(av[i][k], bv[k][n], f);
+          out[i * NN + n] = f;
+          bits = max(bits, __float_as_uint(f));
+        }
+      float* c = C + ((int64_t)b << mnb) + (int64_t)m0 * NN;
+#pragma unroll
+      for (int v = 0; v < NN; ++v)
+        reinterpret_cast<float4*>(c)[v] = make_float4(out[4 * v], out[4 * v + 1], out[4 * v + 2], out[4 * v + 3]);
+      if (m0 == 0) jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - sa - sb;
+    }
+    // Slice maximum: carried per lane group, published when the slice changes
+    // (warp-uniform decisions, as in k_direct).
+    if (__any_sync(0xffffffffu, valid && b != carry_b)) {
+      uint32_t v = carry;
+      for (int off = 1; off < lanes; off <<= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
+      if (carry_b >= 0 && (threadIdx.x & (lanes - 1)) == 0) atomicMax(&jd.c_max[carry_b], v);
+      carry = 0;
+      carry_b = -1;
+    }
+    if (valid) {
+      carry = max(carry, bits);
+      carry_b = b;
+    }
+  }
+  uint32_t v = carry;
+  for (int off = 1; off < lanes; off <<= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
+  if (carry_b >= 0 && (threadIdx.x & (lanes - 1)) == 0) atomicMax(&jd.c_max[carry_b], v);
 }
 
 __device__ __forceinline__ void load4(const float* p, float* v) {
@@ -833,6 +1015,27 @@ int grid_for(int64_t work) {
   return (int)(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
 }
 
+// One resident wave of the staged kernel (contiguous tile ranges need every
+// CTA resident at once to stay balanced), at most one CTA per tile.
+template <class Kern>
+void staged_launch(Kern kern, const JoinDesc& jd, const StageInfo& si, const int64_t* s0, int nslices,
+                   int64_t tiles, size_t bytes, cudaStream_t st) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, bytes) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  const int64_t wave = (int64_t)sms * per_sm;
+  const int grid = (int)(tiles < wave ? tiles : wave);
+  kern<<<grid, kThreads, bytes, st>>>(jd, si, s0, nslices);
+}
+
 // The staged thread-per-output variant applies to K <= 16 when a tile of 2^T
 // (T in [10, 12]) output addresses touches at least 4 rows of each operand
 // (rows are reused) and the staged rows fit 64 KB.  Returns true when launched.
@@ -856,19 +1059,14 @@ bool launch_staged(int mode, const JoinDesc& jd, const int64_t* s0, int nslices,
     si.T = T;
     si.lm = lm;
     si.ln = ln;
+    si.a_inv = jd.a.batch_stride == 0 && jd.a.n_slice_terms == 0;
+    si.b_inv = jd.b.batch_stride == 0 && jd.b.n_slice_terms == 0;
+    si.slice_fast = nslices > 1 && (si.a_inv || si.b_inv);
     const int64_t tiles = (int64_t)nslices << (mnb - T);
-    const int grid = (int)(tiles < 152 * 8 ? tiles : 152 * 8);
-#define TOGB_STAGED(KK)                                                                                   \
-    {                                                                                                     \
-      if (mode == 0) {                                                                                    \
-        cudaFuncSetAttribute(k_direct_staged<0, double, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             64 * 1024);                                                                  \
-        k_direct_staged<0, double, KK><<<grid, kThreads, bytes, st>>>(jd, si, s0, nslices);                \
-      } else {                                                                                            \
-        cudaFuncSetAttribute(k_direct_staged<1, float, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
-                             64 * 1024);                                                                  \
-        k_direct_staged<1, float, KK><<<grid, kThreads, bytes, st>>>(jd, si, s0, nslices);                 \
-      }                                                                                                   \
+#define TOGB_STAGED(KK)                                                                              \
+    {                                                                                                \
+      if (mode == 0) staged_launch(k_direct_staged<0, double, KK>, jd, si, s0, nslices, tiles, bytes, st); \
+      else staged_launch(k_direct_staged<1, float, KK>, jd, si, s0, nslices, tiles, bytes, st);           \
     }
     switch (jd.kb) {
       case 0: TOGB_STAGED(1) break;
@@ -881,6 +1079,60 @@ bool launch_staged(int mode, const JoinDesc& jd, const int64_t* s0, int nslices,
     return true;
   }
   return false;
+}
+
+// Streaming variant (k_stream): split form, natural output, M >= 4, K <= 4,
+// N * K <= 16, A without a leaf residual, and A's four consecutive m either
+// one vector per k or one run with every k, every base offset 16-byte aligned.
+// Returns true when launched.
+bool launch_stream(int mode, const JoinDesc& jd, const int64_t* s0, int nslices, cudaStream_t st) {
+  if (mode != 1 || !jd.c_natural || jd.mb < 2 || jd.kb > 2 || jd.a.ptr_lo) return false;
+  const int K = 1 << jd.kb, N = 1 << jd.nb;
+  if (N * K > 16) return false;
+  const OpDesc& a = jd.a;
+  bool kfast = false;
+  if (a.s_outer[0] == 1 && a.s_outer[1] == 2) {
+    kfast = false;
+  } else if (jd.kb >= 1 && a.s_outer[0] == K && a.s_outer[1] == 2 * K) {
+    for (int j = 0; j < jd.kb; ++j)
+      if (a.s_k[j] != (1ll << j)) return false;
+    kfast = true;
+  } else {
+    return false;
+  }
+  if (((uintptr_t)a.ptr & 15) || ((uintptr_t)jd.c_ptr & 15)) return false;
+  if (a.batch_stride % 4) return false;
+  for (int j = 0; j < a.n_slice_terms; ++j)
+    if (a.slice_stride[j] % 4) return false;
+  for (int i = 2; i < jd.mb; ++i)
+    if (a.s_outer[i] % 4) return false;
+  if (!kfast)
+    for (int j = 0; j < jd.kb; ++j)
+      if (a.s_k[j] % 4) return false;
+  const int64_t quads = (int64_t)nslices << (jd.mb - 2);
+  const int g = grid_for(quads);
+#define TOGB_STREAM(KK, NN)                                                                \
+  {                                                                                        \
+    if (kfast) k_stream<KK, NN, true><<<g, kThreads, 0, st>>>(jd, s0, nslices);            \
+    else k_stream<KK, NN, false><<<g, kThreads, 0, st>>>(jd, s0, nslices);                 \
+  }
+  switch (jd.kb * 8 + jd.nb) {
+    case 0: k_stream<1, 1, false><<<g, kThreads, 0, st>>>(jd, s0, nslices); break;
+    case 1: k_stream<1, 2, false><<<g, kThreads, 0, st>>>(jd, s0, nslices); break;
+    case 2: k_stream<1, 4, false><<<g, kThreads, 0, st>>>(jd, s0, nslices); break;
+    case 3: k_stream<1, 8, false><<<g, kThreads, 0, st>>>(jd, s0, nslices); break;
+    case 4: k_stream<1, 16, false><<<g, kThreads, 0, st>>>(jd, s0, nslices); break;
+    case 8: TOGB_STREAM(2, 1) break;
+    case 9: TOGB_STREAM(2, 2) break;
+    case 10: TOGB_STREAM(2, 4) break;
+    case 11: TOGB_STREAM(2, 8) break;
+    case 16: TOGB_STREAM(4, 1) break;
+    case 17: TOGB_STREAM(4, 2) break;
+    case 18: TOGB_STREAM(4, 4) break;
+    default: return false;
+  }
+#undef TOGB_STREAM
+  return true;
 }
 
 }  // namespace
@@ -911,6 +1163,8 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
       if (mode == 0) k_reduce<0, double><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
       else k_reduce<1, float><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
     }
+  } else if (launch_stream(mode, jd, s0, nslices, st)) {
+    // long operand against a tiny one: streaming variant launched
   } else if (launch_staged(mode, jd, s0, nslices, st)) {
     // short-K join with reused operand rows: staged variant launched
   } else {

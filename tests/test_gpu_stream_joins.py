@@ -1,0 +1,109 @@
+"""Joins of a long intermediate with a tiny leaf -- the joins the split form
+runs on the streaming thread-per-quad kernel.  X (ranks 10-14) is the outer
+product of two seeded dense leaves; the root join contracts it with a dense
+leaf Y of at most 16 entries over k <= 2 shared edges.  The cases are chosen so
+that X's two lowest m bits are either its two lowest address bits or lie just
+above its k bits (the two operand layouts the streaming kernel reads), which
+the host-only lowering confirms without a GPU.  Sliced cases put the slice
+edges on Y and on X (per-slice X) or on Y alone (slice-invariant X, computed
+once and read by every slice).  Tolerances: 1e-12 (plain), 1e-6 (split),
+relative to the largest entry."""
+import numpy as np
+import pytest
+
+from oracle import contract as oracle
+from tensororder_gb300 import runtime
+from tensororder_gb300.program import Leaf, Program
+
+
+def make_program(seed, m, k, n, slices=0, slice_x=True):
+    rng = np.random.default_rng(seed)
+    fa = list(range(m))
+    kk = list(range(m, m + k))
+    fb = list(range(m + k, m + k + n))
+    xa = [int(e) for e in rng.permutation(fa + kk)]
+    ya = [int(e) for e in rng.permutation(kk + fb)]
+    cut = len(xa) // 2
+    sl = [m + k + n + g for g in range(slices)]
+    if slice_x:
+        leaves = [Leaf(xa[:cut] + sl, "dense"), Leaf(xa[cut:], "dense"), Leaf(ya + sl, "dense")]
+        post = [0, 1, -1, 2, -1]
+    else:
+        # slice edges on Y only: Y is the product of two leaves sharing them
+        half = len(ya) // 2
+        leaves = [Leaf(xa[:cut], "dense"), Leaf(xa[cut:], "dense"), Leaf(ya[:half] + sl, "dense"),
+                  Leaf(ya[half:] + sl, "dense")]
+        post = [0, 1, -1, 2, 3, -1, -1]
+    for leaf in leaves:
+        leaf.values = rng.uniform(0.5, 1.5, size=(2,) * leaf.rank)
+    return Program(leaves, post, [[e] for e in sl]).validate()
+
+
+def stream_layout(prog, join):
+    """'mfast' / 'kfast' when the join's A operand has one of the two streaming
+    layouts and its output is natural; None otherwise."""
+    hp = runtime.HostProgram(prog)
+    try:
+        txt = hp.describe(runtime.MODE_SPLIT, join)
+    finally:
+        hp.close()
+    head = txt.splitlines()[0].split()
+    natural = int(head[head.index("c_natural") + 1])
+    mb, nb, kb = (int(x) for x in head[3:6])
+    so = sk = None
+    a_lo = False
+    for line in txt.splitlines():
+        t = line.split()
+        if t[:2] == ["A", "s_outer"]:
+            so = [int(x) for x in t[2:]]
+        if t[:2] == ["A", "s_k"]:
+            sk = [int(x) for x in t[2:]]
+        if t[:2] == ["A", "leaf"]:
+            a_lo = int(t[2]) == 1
+    if not natural or a_lo or kb > 2 or (1 << (nb + kb)) > 16 or mb < 2:
+        return None
+    K = 1 << kb
+    if so[:2] == [1, 2]:
+        return "mfast"
+    if kb >= 1 and so[:2] == [K, 2 * K] and sk == [1 << j for j in range(kb)]:
+        return "kfast"
+    return None
+
+
+# (seed, m, k, n, slices, slice_x, layout)
+CASES = [
+    (0, 12, 1, 2, 0, True, "mfast"), (13, 12, 1, 2, 0, True, "kfast"), (0, 13, 2, 1, 0, True, "mfast"),
+    (0, 12, 0, 4, 0, True, "mfast"), (1, 11, 2, 2, 0, True, "mfast"), (39, 11, 2, 2, 0, True, "kfast"),
+    (4, 14, 1, 3, 0, True, "kfast"), (2, 14, 1, 3, 0, True, "mfast"), (3, 10, 2, 0, 0, True, "mfast"),
+    (1, 12, 1, 2, 2, True, "mfast"), (32, 12, 1, 2, 2, True, "kfast"), (5, 13, 2, 1, 3, True, "mfast"),
+    (6, 14, 1, 3, 2, True, "kfast"), (2, 12, 0, 4, 2, True, "mfast"),
+    (0, 12, 1, 2, 3, False, "mfast"), (13, 12, 1, 2, 2, False, "kfast"), (4, 14, 1, 3, 3, False, "kfast"),
+    (1, 13, 2, 1, 2, False, "mfast"), (3, 12, 0, 4, 2, False, "mfast"),
+]
+
+
+def _prog(case):
+    seed, m, k, n, slices, slice_x, _ = case
+    return make_program(seed, m, k, n, slices, slice_x)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_cases_have_the_streaming_layout(case):
+    """Host-only lowering: the root join of every case is a streaming join."""
+    prog = _prog(case)
+    assert stream_layout(prog, prog.postorder.count(-1) - 1) == case[-1]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("mode,tol", [(runtime.MODE_F64, 1e-12), (runtime.MODE_SPLIT, 1e-6)])
+def test_stream_join(case, mode, tol, cuda):
+    prog = _prog(case)
+    want = sum(oracle.contract(prog, s)[0] for s in range(prog.num_slices))
+    dp = runtime.DeviceProgram(prog)
+    dp.reset()
+    dp.run(mode)
+    got = dp.result()
+    dp.close()
+    assert got.shape == want.shape
+    assert np.abs(got - want).max() <= tol * np.abs(want).max()
