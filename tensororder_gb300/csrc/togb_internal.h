@@ -87,6 +87,47 @@ void make_runs(const int64_t* s, int nbits, Runs* out);
 // (strides s[0..nbits)) back to that index's bits.
 void make_inverse_runs(const int64_t* s, int nbits, Runs* out);
 
+// Fused slice-invariant joins: one launch runs a topologically ordered list
+// of thread-per-output joins.  Each join's outputs are cut into tiles of
+// kOnceTile; CTAs claim tiles in list order from a global counter and, before
+// computing a tile, wait (bounded) until every tile of the joins it reads has
+// been published.  A CTA only ever waits for tiles claimed before its own, by
+// CTAs that are running, so the launch needs no co-residency.
+constexpr int kOnceTile = 1024;  // outputs per tile (256 threads x 4)
+// The fields of a JoinDesc a fused join needs (slice-invariant joins read no
+// slice offsets), small enough to be copied to shared memory per tile.
+struct OnceJoin {
+  const void* a;
+  const void* b;
+  const float* a_lo;         // split form, leaves: residual planes (or null)
+  const float* b_lo;
+  void* c;
+  const uint32_t* a_max;     // split form, intermediates: max bits (null for leaves)
+  const uint32_t* b_max;
+  const int32_t* a_exp;
+  const int32_t* b_exp;
+  int32_t* c_exp;
+  uint32_t* c_max;
+  int32_t a_shift, b_shift;  // split form, leaves: power-of-two normaliser
+  int32_t mb, nb, kb, natural;
+  int32_t a_ktab[16], b_ktab[16];
+  Runs a_outer, b_outer, a_k, b_k, inv_m, inv_n;
+};
+struct OnceList {
+  const OnceJoin* joins;     // device [n]
+  const int32_t* tile_join;  // device [total_tiles]: list index of each tile's join
+  const int32_t* tile_first; // device [n + 1]: first tile of each join
+  const int32_t* deps;       // device [2n]: list index of the A / B producer within the list, or -1
+  int32_t n;
+  int32_t total_tiles;
+  uint32_t* counters;        // device [1 + n]: next tile, then published tiles per join (zero before the launch)
+  int32_t* err;              // set when a wait expires
+};
+cudaError_t launch_once_list(int mode, const OnceList& ol, cudaStream_t st);
+
+// Which thread-per-output variant a K_DIRECT join runs: 0 k_direct,
+// 1 k_direct_staged, 2 k_stream (m-fast A), 3 k_stream (k-fast A).
+int direct_variant(int mode, const JoinDesc& jd);
 // Launchers (togb_kernels.cu).  `s0` points at the global index of the first
 // slice of the chunk; `nslices` is the number of slices in the chunk.
 cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t* s0, int nslices,

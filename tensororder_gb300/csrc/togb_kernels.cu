@@ -222,8 +222,9 @@ __global__ void __launch_bounds__(kThreads) k_direct(const __grid_constant__ Joi
 // Each CTA takes tiles of 2^T consecutive output addresses of one slice.  The
 // T lowest address bits belong to lm bits of m and ln bits of n (lm + ln = T),
 // so a tile reads just 2^lm rows of A and 2^ln rows of B: the CTA loads those
-// rows (K values each) into shared memory, then every thread computes four
-// consecutive outputs from shared memory and stores them as one vector.
+// rows (K values each; in the split form already scaled to the slice maximum)
+// into shared memory, then every thread computes four consecutive outputs from
+// shared memory and stores them as one vector.
 // Output addresses are dense per slice, so a tile is one contiguous run.
 // When one operand does not vary with the slice, every CTA walks a contiguous
 // range of tiles with the slice index fastest and keeps that operand's rows
@@ -328,6 +329,12 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
   // published (one atomic per warp) only when the slice changes.
   uint32_t carry = 0;
   int carry_b = -1;
+  int ja[4], jb[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    ja[j] = IA[0][j];
+    jb[j] = IB[0][j];
+  }
   int64_t staged_pos = -1;  // tile position whose rows are staged
   int staged_b = -1;        // slice whose rows are staged
   for (int64_t t = t_begin; t < t_end; t += t_step) {
@@ -368,8 +375,12 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
         for (int e = threadIdx.x; e < rowsA * KK; e += blockDim.x) {
           const int r = e / KK, k = e - r * KK;
           const int64_t o = baseA + offA[r] + jd.a.ktab[k];
-          As[e] = A[o];
-          if (MODE == 1 && jd.a.ptr_lo) Alo[e] = ((const float*)jd.a.ptr_lo)[o];
+          if (MODE == 1) {  // staged already scaled (exact powers of two)
+            As[e] = (T)((float)A[o] * fa);
+            if (jd.a.ptr_lo) Alo[e] = ((const float*)jd.a.ptr_lo)[o] * fa;
+          } else {
+            As[e] = A[o];
+          }
         }
       }
       if (newB) {
@@ -377,8 +388,12 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
         for (int e = threadIdx.x; e < rowsB * KK; e += blockDim.x) {
           const int r = e / KK, k = e - r * KK;
           const int64_t o = baseB + offB[r] + jd.b.ktab[k];
-          Bs[e] = B[o];
-          if (MODE == 1 && jd.b.ptr_lo) Blo[e] = ((const float*)jd.b.ptr_lo)[o];
+          if (MODE == 1) {
+            Bs[e] = (T)((float)B[o] * fb);
+            if (jd.b.ptr_lo) Blo[e] = ((const float*)jd.b.ptr_lo)[o] * fb;
+          } else {
+            Bs[e] = B[o];
+          }
         }
       }
       staged_pos = pos;
@@ -389,12 +404,15 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
 #pragma unroll 1
     for (int i = 0; i < per_thread; ++i) {
       const int q0 = 4 * (threadIdx.x + kThreads * i);
+      // The row tables are OR-linear in the address bits: the two lowest
+      // bits (j) contribute IA[0][j] / IB[0][j] to every group.
+      const int ra0 = IA[0][q0 & 63] | IA[1][(q0 >> 6) & 63];
+      const int rb0 = IB[0][q0 & 63] | IB[1][(q0 >> 6) & 63];
       T out[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        const int q = q0 + j;
-        const int ra = IA[0][q & 63] | IA[1][(q >> 6) & 63];
-        const int rb = IB[0][q & 63] | IB[1][(q >> 6) & 63];
+        const int ra = ra0 | ja[j];
+        const int rb = rb0 | jb[j];
         T ar[KK], br[KK];
         lds_row<T, KK>(As + ra * KK, ar);
         lds_row<T, KK>(Bs + rb * KK, br);
@@ -404,16 +422,16 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
             float al[KK];
             lds_row<float, KK>(Alo + ra * KK, al);
 #pragma unroll
-            for (int k = 0; k < KK; ++k) f = fmaf(al[k] * fa, (float)br[k] * fb, f);
+            for (int k = 0; k < KK; ++k) f = fmaf(al[k], (float)br[k], f);
           }
           if (jd.b.ptr_lo) {
             float bl[KK];
             lds_row<float, KK>(Blo + rb * KK, bl);
 #pragma unroll
-            for (int k = 0; k < KK; ++k) f = fmaf((float)ar[k] * fa, bl[k] * fb, f);
+            for (int k = 0; k < KK; ++k) f = fmaf((float)ar[k], bl[k], f);
           }
 #pragma unroll
-          for (int k = 0; k < KK; ++k) f = fmaf((float)ar[k] * fa, (float)br[k] * fb, f);
+          for (int k = 0; k < KK; ++k) f = fmaf((float)ar[k], (float)br[k], f);
           out[j] = (T)f;
           bits = max(bits, __float_as_uint(f));
         } else {
@@ -551,6 +569,267 @@ __global__ void __launch_bounds__(kThreads) k_stream(const __grid_constant__ Joi
   uint32_t v = carry;
   for (int off = 1; off < lanes; off <<= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
   if (carry_b >= 0 && (threadIdx.x & (lanes - 1)) == 0) atomicMax(&jd.c_max[carry_b], v);
+}
+
+// ---------------------------------------------------------------------------
+// Fused slice-invariant joins (OnceList).  Operands written earlier in the
+// same launch by other CTAs are read through L2 (ld.global.cg): L1 is not
+// coherent, and the arena of a fused list is never reused, so no stale line
+// can be hit.  The arithmetic of every output is dot_k's (the KK > 0 order for
+// K <= 16, the compensated 16-term chunks above), so the results equal the
+// unfused launches bit for bit.
+
+constexpr long long kOnceWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Operand values of one output for K <= KMAX (split form: already scaled),
+// every load issued before any is used.
+template <int MODE, class T, int KMAX>
+__device__ __forceinline__ void once_load(const OnceJoin& oj, int64_t oa, int64_t ob, int K, float fa, float fb,
+                                          T* av, T* bv, float* al, float* bl) {
+#pragma unroll
+  for (int k = 0; k < KMAX; ++k) {
+    if (k < K) {
+      const T x = __ldcg((const T*)oj.a + oa + oj.a_ktab[k]);
+      const T y = __ldcg((const T*)oj.b + ob + oj.b_ktab[k]);
+      if (MODE == 1) {
+        av[k] = (T)((float)x * fa);
+        bv[k] = (T)((float)y * fb);
+        al[k] = oj.a_lo ? __ldcg(oj.a_lo + oa + oj.a_ktab[k]) * fa : 0.f;
+        bl[k] = oj.b_lo ? __ldcg(oj.b_lo + ob + oj.b_ktab[k]) * fb : 0.f;
+      } else {
+        av[k] = x;
+        bv[k] = y;
+      }
+    }
+  }
+}
+
+// dot_k's KK > 0 order on loaded values: A residual terms, B residual terms,
+// then the main terms.
+template <int MODE, class T, int KMAX>
+__device__ __forceinline__ T once_dot(const OnceJoin& oj, int K, const T* av, const T* bv, const float* al,
+                                      const float* bl) {
+  if (MODE == 1) {
+    float f = 0.f;
+    if (oj.a_lo) {
+#pragma unroll
+      for (int k = 0; k < KMAX; ++k)
+        if (k < K) f = fmaf(al[k], (float)bv[k], f);
+    }
+    if (oj.b_lo) {
+#pragma unroll
+      for (int k = 0; k < KMAX; ++k)
+        if (k < K) f = fmaf((float)av[k], bl[k], f);
+    }
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k)
+      if (k < K) f = fmaf((float)av[k], (float)bv[k], f);
+    return (T)f;
+  } else {
+    T acc = 0;
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k)
+      if (k < K) acc = fma(av[k], bv[k], acc);
+    return acc;
+  }
+}
+
+// 8 < K <= 16: the KK > 0 order with the loads inside each pass.
+template <int MODE, class T>
+__device__ T once_dot_serial(const OnceJoin& oj, int64_t oa, int64_t ob, int K, float fa, float fb) {
+  const T* A = (const T*)oj.a;
+  const T* B = (const T*)oj.b;
+  if (MODE == 1) {
+    float f = 0.f;
+    if (oj.a_lo)
+      for (int k = 0; k < K; ++k)
+        f = fmaf(__ldcg(oj.a_lo + oa + oj.a_ktab[k]) * fa, (float)__ldcg(B + ob + oj.b_ktab[k]) * fb, f);
+    if (oj.b_lo)
+      for (int k = 0; k < K; ++k)
+        f = fmaf((float)__ldcg(A + oa + oj.a_ktab[k]) * fa, __ldcg(oj.b_lo + ob + oj.b_ktab[k]) * fb, f);
+    for (int k = 0; k < K; ++k)
+      f = fmaf((float)__ldcg(A + oa + oj.a_ktab[k]) * fa, (float)__ldcg(B + ob + oj.b_ktab[k]) * fb, f);
+    return (T)f;
+  } else {
+    T acc = 0;
+    for (int k = 0; k < K; ++k) acc = fma(__ldcg(A + oa + oj.a_ktab[k]), __ldcg(B + ob + oj.b_ktab[k]), acc);
+    return acc;
+  }
+}
+
+// K > 16: dot_k's compensated 16-term chunks (split form), k offsets from the runs.
+template <int MODE, class T>
+__device__ T once_dot_long(const OnceJoin& oj, int64_t oa, int64_t ob, int K, float fa, float fb) {
+  const T* A = (const T*)oj.a;
+  const T* B = (const T*)oj.b;
+  if (MODE == 1) {
+    float sum = 0.f, comp = 0.f;
+    for (int k0 = 0; k0 < K; k0 += 16) {
+      float f = 0.f;
+      for (int k = k0; k < k0 + 16 && k < K; ++k) {
+        const int64_t ka = dep(oj.a_k, (uint64_t)k), kb = dep(oj.b_k, (uint64_t)k);
+        const float av = (float)__ldcg(A + oa + ka) * fa, bv = (float)__ldcg(B + ob + kb) * fb;
+        if (oj.a_lo) f = fmaf(__ldcg(oj.a_lo + oa + ka) * fa, bv, f);
+        if (oj.b_lo) f = fmaf(av, __ldcg(oj.b_lo + ob + kb) * fb, f);
+        f = fmaf(av, bv, f);
+      }
+      const float t = sum + f;
+      comp += fabsf(sum) >= fabsf(f) ? (sum - t) + f : (f - t) + sum;
+      sum = t;
+    }
+    return (T)(sum + comp);
+  } else {
+    T acc = 0;
+    for (int k = 0; k < K; ++k)
+      acc = fma(__ldcg(A + oa + dep(oj.a_k, (uint64_t)k)), __ldcg(B + ob + dep(oj.b_k, (uint64_t)k)), acc);
+    return acc;
+  }
+}
+
+template <int MODE, class T>
+__global__ void __launch_bounds__(kThreads, 3) k_once_list(const __grid_constant__ OnceList ol) {
+  __shared__ __align__(16) OnceJoin sj;
+  __shared__ int s_tile, s_join, s_bad;
+  __shared__ uint32_t s_bits[kThreads / 32];
+  volatile int32_t* err = ol.err;
+  int cur = -1;  // join whose descriptor is in shared memory (block-uniform)
+  int pre = -1;  // thread 0: the next tile, claimed while the current one is computed
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int t = pre >= 0 ? pre : (int)atomicAdd(ol.counters, 1u);
+      pre = -1;
+      int j = -1, bad = 0;
+      if (t < ol.total_tiles) {
+        j = ol.tile_join[t];
+        const int da = ol.deps[2 * j], db = ol.deps[2 * j + 1];
+        const uint32_t na = da >= 0 ? (uint32_t)(ol.tile_first[da + 1] - ol.tile_first[da]) : 0u;
+        const uint32_t nb = db >= 0 ? (uint32_t)(ol.tile_first[db + 1] - ol.tile_first[db]) : 0u;
+        const long long t0 = clock64();
+        for (;;) {
+          const uint32_t ga = da >= 0 ? ld_acquire_u32(ol.counters + 1 + da) : 0u;
+          const uint32_t gb = db >= 0 ? ld_acquire_u32(ol.counters + 1 + db) : 0u;
+          if (ga >= na && gb >= nb) break;
+          if (*err || clock64() - t0 > kOnceWaitCycles) {
+            bad = 1;
+            break;
+          }
+        }
+        if (bad) atomicExch((int*)ol.err, 1);
+        __threadfence();
+      }
+      s_tile = t;
+      s_join = j;
+      s_bad = bad;
+    }
+    __syncthreads();
+    const int j = s_join;
+    if (j < 0 || s_bad) return;  // block-uniform
+    // Claiming ahead keeps the order argument: the claimed tile is started as
+    // soon as this one is published.
+    if (threadIdx.x == 0) pre = (int)atomicAdd(ol.counters, 1u);
+    const int tile = s_tile - ol.tile_first[j];
+    if (j != cur) {
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(ol.joins + j);
+      uint32_t* dst = reinterpret_cast<uint32_t*>(&sj);
+      for (int i = threadIdx.x; i < (int)(sizeof(OnceJoin) / 4); i += kThreads) dst[i] = src[i];
+      __syncthreads();
+      cur = j;
+    }
+    const int mnb = sj.mb + sj.nb;
+    const int64_t outs = 1ll << mnb;
+    const int64_t q0 = (int64_t)tile * kOnceTile + 4 * threadIdx.x;
+    uint32_t bits = 0;
+    if (q0 < outs) {
+      const uint64_t nmask = (1ull << sj.nb) - 1;
+      int sa = 0, sb = 0;
+      float fa = 1.f, fb = 1.f;
+      if (MODE == 1) {
+        sa = sj.a_max ? shift_from_max(__ldcg(sj.a_max)) : sj.a_shift;
+        sb = sj.b_max ? shift_from_max(__ldcg(sj.b_max)) : sj.b_shift;
+        fa = pow2f(sa);
+        fb = pow2f(sb);
+      }
+      const int K = 1 << sj.kb;
+      const int cnt = outs - q0 < 4 ? (int)(outs - q0) : 4;
+      // Operand offsets of output q0 + v (q0 itself past the end of the join).
+      auto offsets = [&](int v, int64_t& oa, int64_t& ob) {
+        const uint64_t q = (uint64_t)(q0 + (v < cnt ? v : 0));
+        const uint64_t m = sj.natural ? (q >> sj.nb) : (uint64_t)dep(sj.inv_m, q);
+        const uint64_t n = sj.natural ? (q & nmask) : (uint64_t)dep(sj.inv_n, q);
+        oa = dep(sj.a_outer, m);
+        ob = dep(sj.b_outer, n);
+      };
+      T out[4];
+      if (K <= 4) {  // independent outputs: the compiler overlaps their loads
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          int64_t oa, ob;
+          offsets(v, oa, ob);
+          T av[4], bv[4];
+          float al[4], bl[4];
+          once_load<MODE, T, 4>(sj, oa, ob, K, fa, fb, av, bv, al, bl);
+          out[v] = once_dot<MODE, T, 4>(sj, K, av, bv, al, bl);
+        }
+      } else if (K <= 8) {
+#pragma unroll 1
+        for (int v = 0; v < 4; ++v) {
+          int64_t oa, ob;
+          offsets(v, oa, ob);
+          T av[8], bv[8];
+          float al[8], bl[8];
+          once_load<MODE, T, 8>(sj, oa, ob, K, fa, fb, av, bv, al, bl);
+          out[v] = once_dot<MODE, T, 8>(sj, K, av, bv, al, bl);
+        }
+      } else if (K <= 16) {
+#pragma unroll 1
+        for (int v = 0; v < 4; ++v) {
+          int64_t oa, ob;
+          offsets(v, oa, ob);
+          out[v] = once_dot_serial<MODE, T>(sj, oa, ob, K, fa, fb);
+        }
+      } else {
+#pragma unroll 1
+        for (int v = 0; v < 4; ++v) {
+          int64_t oa, ob;
+          offsets(v, oa, ob);
+          out[v] = once_dot_long<MODE, T>(sj, oa, ob, K, fa, fb);
+        }
+      }
+      T* C = (T*)sj.c;
+      if (cnt == 4) {
+        store_vec(C + q0, out);
+      } else {
+        for (int v = 0; v < cnt; ++v) C[q0 + v] = out[v];
+      }
+      if (MODE == 1) {
+        for (int v = 0; v < cnt; ++v) bits = max(bits, __float_as_uint((float)out[v]));
+        if (q0 == 0) {
+          const int ea = sj.a_exp ? __ldcg(sj.a_exp) : 0, eb = sj.b_exp ? __ldcg(sj.b_exp) : 0;
+          *sj.c_exp = ea + eb - sa - sb;
+        }
+      }
+    }
+    if (MODE == 1) {
+      for (int off = 16; off > 0; off >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, off));
+      if ((threadIdx.x & 31) == 0) s_bits[threadIdx.x >> 5] = bits;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (MODE == 1) {
+        uint32_t v = 0;
+        for (int w = 0; w < kThreads / 32; ++w) v = max(v, s_bits[w]);
+        if (v) atomicMax(sj.c_max, v);
+      }
+      __threadfence();
+      atomicAdd(ol.counters + 1 + j, 1u);
+    }
+  }
 }
 
 __device__ __forceinline__ void load4(const float* p, float* v) {
@@ -1039,20 +1318,20 @@ void staged_launch(Kern kern, const JoinDesc& jd, const StageInfo& si, const int
 // The staged thread-per-output variant applies to K <= 16 when a tile of 2^T
 // (T in [10, 12]) output addresses touches at least 4 rows of each operand
 // (rows are reused) and the staged rows fit 64 KB.  Returns true when launched.
-bool launch_staged(int mode, const JoinDesc& jd, const int64_t* s0, int nslices, cudaStream_t st) {
+bool staged_plan(int mode, const JoinDesc& jd, StageInfo& si, size_t& bytes) {
   const int mnb = jd.mb + jd.nb;
   if (jd.kb > 4 || mnb < 10) return false;
   const int K = 1 << jd.kb;
   const size_t es = mode == 0 ? 8 : 4;
-  StageInfo si{};
   for (int T = mnb < 12 ? mnb : 12; T >= 10; --T) {
+    si = StageInfo{};
     int lm = 0, ln = 0;
     for (int i = 0; i < jd.mb; ++i)
       if (jd.c_s_m[i] < (1ll << T)) si.a_row_bits[lm++] = i;
     for (int i = 0; i < jd.nb; ++i)
       if (jd.c_s_n[i] < (1ll << T)) si.b_row_bits[ln++] = i;
     if (lm + ln != T || lm < 2 || ln < 2) continue;
-    size_t bytes = ((size_t)1 << lm) * K * es + ((size_t)1 << ln) * K * es;
+    bytes = ((size_t)1 << lm) * K * es + ((size_t)1 << ln) * K * es;
     if (mode == 1) bytes += (jd.a.ptr_lo ? ((size_t)1 << lm) * K * 4 : 0) + (jd.b.ptr_lo ? ((size_t)1 << ln) * K * 4 : 0);
     bytes += 4 * (((size_t)1 << lm) + ((size_t)1 << ln));  // row offsets
     if (bytes > 64 * 1024) continue;
@@ -1061,36 +1340,42 @@ bool launch_staged(int mode, const JoinDesc& jd, const int64_t* s0, int nslices,
     si.ln = ln;
     si.a_inv = jd.a.batch_stride == 0 && jd.a.n_slice_terms == 0;
     si.b_inv = jd.b.batch_stride == 0 && jd.b.n_slice_terms == 0;
-    si.slice_fast = nslices > 1 && (si.a_inv || si.b_inv);
-    const int64_t tiles = (int64_t)nslices << (mnb - T);
-#define TOGB_STAGED(KK)                                                                              \
-    {                                                                                                \
-      if (mode == 0) staged_launch(k_direct_staged<0, double, KK>, jd, si, s0, nslices, tiles, bytes, st); \
-      else staged_launch(k_direct_staged<1, float, KK>, jd, si, s0, nslices, tiles, bytes, st);           \
-    }
-    switch (jd.kb) {
-      case 0: TOGB_STAGED(1) break;
-      case 1: TOGB_STAGED(2) break;
-      case 2: TOGB_STAGED(4) break;
-      case 3: TOGB_STAGED(8) break;
-      default: TOGB_STAGED(16) break;
-    }
-#undef TOGB_STAGED
     return true;
   }
   return false;
+}
+
+bool launch_staged(int mode, const JoinDesc& jd, const int64_t* s0, int nslices, cudaStream_t st) {
+  StageInfo si;
+  size_t bytes = 0;
+  if (!staged_plan(mode, jd, si, bytes)) return false;
+  si.slice_fast = nslices > 1 && (si.a_inv || si.b_inv);
+  const int64_t tiles = (int64_t)nslices << (jd.mb + jd.nb - si.T);
+#define TOGB_STAGED(KK)                                                                                    \
+  {                                                                                                        \
+    if (mode == 0) staged_launch(k_direct_staged<0, double, KK>, jd, si, s0, nslices, tiles, bytes, st);   \
+    else staged_launch(k_direct_staged<1, float, KK>, jd, si, s0, nslices, tiles, bytes, st);              \
+  }
+  switch (jd.kb) {
+    case 0: TOGB_STAGED(1) break;
+    case 1: TOGB_STAGED(2) break;
+    case 2: TOGB_STAGED(4) break;
+    case 3: TOGB_STAGED(8) break;
+    default: TOGB_STAGED(16) break;
+  }
+#undef TOGB_STAGED
+  return true;
 }
 
 // Streaming variant (k_stream): split form, natural output, M >= 4, K <= 4,
 // N * K <= 16, A without a leaf residual, and A's four consecutive m either
 // one vector per k or one run with every k, every base offset 16-byte aligned.
 // Returns true when launched.
-bool launch_stream(int mode, const JoinDesc& jd, const int64_t* s0, int nslices, cudaStream_t st) {
+bool stream_ok(int mode, const JoinDesc& jd, bool& kfast) {
   if (mode != 1 || !jd.c_natural || jd.mb < 2 || jd.kb > 2 || jd.a.ptr_lo) return false;
   const int K = 1 << jd.kb, N = 1 << jd.nb;
   if (N * K > 16) return false;
   const OpDesc& a = jd.a;
-  bool kfast = false;
   if (a.s_outer[0] == 1 && a.s_outer[1] == 2) {
     kfast = false;
   } else if (jd.kb >= 1 && a.s_outer[0] == K && a.s_outer[1] == 2 * K) {
@@ -1109,6 +1394,12 @@ bool launch_stream(int mode, const JoinDesc& jd, const int64_t* s0, int nslices,
   if (!kfast)
     for (int j = 0; j < jd.kb; ++j)
       if (a.s_k[j] % 4) return false;
+  return true;
+}
+
+bool launch_stream(int mode, const JoinDesc& jd, const int64_t* s0, int nslices, cudaStream_t st) {
+  bool kfast = false;
+  if (!stream_ok(mode, jd, kfast)) return false;
   const int64_t quads = (int64_t)nslices << (jd.mb - 2);
   const int g = grid_for(quads);
 #define TOGB_STREAM(KK, NN)                                                                \
@@ -1136,6 +1427,14 @@ bool launch_stream(int mode, const JoinDesc& jd, const int64_t* s0, int nslices,
 }
 
 }  // namespace
+
+int direct_variant(int mode, const JoinDesc& jd) {
+  bool kfast = false;
+  if (stream_ok(mode, jd, kfast)) return kfast ? 3 : 2;
+  StageInfo si;
+  size_t bytes = 0;
+  return staged_plan(mode, jd, si, bytes) ? 1 : 0;
+}
 
 cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t* s0, int nslices,
                         cudaStream_t st) {
@@ -1190,6 +1489,26 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
     }
 #undef TOGB_DIRECT
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_once_list(int mode, const OnceList& ol, cudaStream_t st) {
+  if (ol.n <= 0 || ol.total_tiles <= 0) return cudaSuccess;
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  int per_sm = 0;
+  cudaError_t e = mode == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<0, double>, kThreads, 0)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<1, float>, kThreads, 0);
+  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+  const int64_t wave = (int64_t)sms * per_sm;
+  const int grid = (int)(ol.total_tiles < wave ? ol.total_tiles : wave);
+  if (mode == 0) k_once_list<0, double><<<grid, kThreads, 0, st>>>(ol);
+  else k_once_list<1, float><<<grid, kThreads, 0, st>>>(ol);
   return cudaGetLastError();
 }
 

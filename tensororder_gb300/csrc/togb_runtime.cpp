@@ -122,6 +122,13 @@ void togb::make_inverse_runs(const int64_t* s, int nbits, Runs* out) {
   }
 }
 
+// One step of the slice-invariant phase: a fused OnceList of joins, or one join.
+struct OnceSeg {
+  bool fused = false;
+  std::vector<int> js;  // indices into joins, in execution order
+  togb::OnceList ol{};
+};
+
 struct togb_program {
   int device = 0;
   int G = 0;
@@ -167,6 +174,17 @@ struct togb_program {
   size_t max_bytes = 0;
   uint32_t* d_max_once = nullptr;  // split mode max bits [slice-invariant joins]
   size_t max_once_bytes = 0;
+  // Fused slice-invariant phase: runs of consecutive thread-per-output joins
+  // of `once` become one OnceList launch each (the other joins stay single
+  // launches).  Possible when the slice-invariant arena is planned without
+  // reuse (no join overwrites an operand another join may still read).
+  bool allow_fused_once = true;  // false for the allocation-free entry point
+  bool once_no_reuse = false;
+  std::vector<OnceSeg> once_segs;
+  int once_segs_mode = -1;          // form the segments were built for, -1 = none
+  uint32_t* d_once_ctr = nullptr;   // tile counters of every fused segment
+  size_t once_ctr_bytes = 0;
+  std::vector<void*> once_bufs;     // device copies of the segments' tables (freed with the program)
   std::map<int, cudaGraphExec_t> graphs;  // by chunk slice count
   bool use_graphs = true;
   bool timing = false;
@@ -337,6 +355,7 @@ int64_t plan_phase_arena(togb_program* p, bool dep) {
     if (J.dep != dep) continue;
     const int64_t size = (pow2(J.rank) + kAlignElems - 1) / kAlignElems * kAlignElems;
     J.off = alloc(size);
+    if (!dep && p->once_no_reuse) continue;  // fused slice-invariant phase: every output keeps its place
     for (int opnd : {J.left, J.right}) {
       const Node& O = p->nodes[opnd];
       if (O.leaf < 0 && O.dep == dep) release(O.off);
@@ -361,6 +380,11 @@ void plan_arena(togb_program* p) {
     (J.dep ? p->flops : p->flops_once) += 2.0 * M * N * K;
     (J.dep ? p->bytes64 : p->bytes64_once) += 8.0 * (M * K + K * N + M * N);
   }
+  // The slice-invariant outputs keep their places (so the phase can run as
+  // fused lists) unless that needs more than 2^24 elements.
+  int64_t once_total = 0;
+  for (int j : p->once) once_total += (pow2(p->nodes[p->joins[j]].rank) + kAlignElems - 1) / kAlignElems * kAlignElems;
+  p->once_no_reuse = p->allow_fused_once && once_total <= (int64_t(1) << 24);
   p->arena = std::max<int64_t>(plan_phase_arena(p, true), kAlignElems);
   p->arena_once = plan_phase_arena(p, false);
 }
@@ -559,6 +583,8 @@ void swap_operands(JoinDesc& jd) {
 }
 
 void build_descs(togb_program* p, int mode, void* ws_v, int B) {
+  p->once_segs_mode = -1;  // fused slice-invariant lists follow the descriptors
+  p->once_segs.clear();
   char* ws = (char*)ws_v;
   const size_t es = elem_size(mode);
   p->jds.assign(p->joins.size(), JoinDesc{});
@@ -617,6 +643,169 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
   }
 }
 
+// Splits the slice-invariant joins of the current descriptors into fused
+// lists (runs of consecutive thread-per-output joins) and single launches, and
+// copies each list's tables to the device.  Tables of earlier builds stay
+// allocated until the program is destroyed: a batch graph captured from them
+// may still be launched.
+togb_status prepare_once_fused(togb_program* p, int mode) {
+  if (p->once_segs_mode == mode) return TOGB_OK;
+  p->once_segs.clear();
+  p->once_segs_mode = -1;
+  if (!p->once_no_reuse || p->once.empty()) {
+    p->once_segs_mode = mode;
+    return TOGB_OK;
+  }
+  // Every join as early as its producers allow, in the order F0 N0 F1 N1 ...
+  // (F: fused lists of thread-per-output joins, N: the other joins, one
+  // launch each).  A thread-per-output join goes to the first F after all of
+  // its producers, any other join to the first N after them.  Inside an F the
+  // joins are ordered by depth, so a claimed tile waits only for joins whose
+  // tiles were claimed (and mostly finished) well before it.
+  std::unordered_map<int, int> place, depth;  // join -> step index (F_s = 2s, N_t = 2t + 1), depth in its F
+  int steps = 0;
+  for (int j : p->once) {
+    const Node& J = p->nodes[p->joins[j]];
+    const bool direct = join_kernel(p, J, mode) == togb::K_DIRECT;
+    int at = direct ? 0 : 1, d = 0;
+    for (int opnd : {J.left, J.right}) {
+      const Node& O = p->nodes[opnd];
+      if (O.leaf >= 0 || O.dep) continue;
+      const int pi = place.at(O.join);
+      // an F join may share its producer's F (the list waits) and follows an
+      // N producer in the next F; an N join follows an F producer in the
+      // next N and may share an N producer's step (launched after it)
+      const int need = direct ? (pi % 2 == 0 ? pi : pi + 1) : (pi % 2 == 0 ? pi + 1 : pi);
+      at = std::max(at, need);
+      if (direct && need == pi) d = std::max(d, depth.at(O.join) + 1);
+    }
+    place[j] = at;
+    depth[j] = d;
+    steps = std::max(steps, at + 1);
+  }
+  for (int st = 0; st < steps; ++st) {
+    std::vector<std::pair<int, int>> members;  // (depth, position in once) of the joins of this step
+    for (size_t i = 0; i < p->once.size(); ++i)
+      if (place[p->once[i]] == st) members.push_back({st % 2 == 0 ? depth[p->once[i]] : 0, (int)i});
+    if (members.empty()) continue;
+    std::stable_sort(members.begin(), members.end());
+    if (st % 2 == 0) {
+      p->once_segs.emplace_back();
+      p->once_segs.back().fused = true;
+      for (auto& m : members) p->once_segs.back().js.push_back(p->once[m.second]);
+    } else {
+      for (auto& m : members) {
+        p->once_segs.emplace_back();
+        p->once_segs.back().fused = false;
+        p->once_segs.back().js.push_back(p->once[m.second]);
+      }
+    }
+  }
+  // Host images of the tables: [OnceJoin x n][tile_first x (n + 1)][deps x 2n][tile_join x tiles],
+  // 256-byte aligned pieces.
+  std::vector<char> img;
+  size_t ctr = 0;
+  auto put = [&img](const void* src, size_t bytes) {
+    const size_t off = (img.size() + 255) / 256 * 256;
+    img.resize(off + bytes);
+    std::memcpy(img.data() + off, src, bytes);
+    return off;
+  };
+  const size_t G = p->once_segs.size();
+  std::vector<size_t> off_j(G), off_tf(G), off_dep(G), off_tj(G), off_ctr(G);
+  for (size_t g = 0; g < G; ++g) {
+    OnceSeg& S = p->once_segs[g];
+    if (!S.fused) continue;
+    const int n = (int)S.js.size();
+    std::unordered_map<int, int> local;
+    for (int i = 0; i < n; ++i) local[S.js[i]] = i;
+    std::vector<togb::OnceJoin> oj(n);
+    std::vector<int32_t> tf(n + 1, 0), deps(2 * n, -1), tj;
+    for (int i = 0; i < n; ++i) {
+      const Node& J = p->nodes[p->joins[S.js[i]]];
+      const JoinDesc& jd = p->jds[S.js[i]];
+      togb::OnceJoin& o = oj[i];
+      std::memset(&o, 0, sizeof(o));
+      o.a = jd.a.ptr;
+      o.b = jd.b.ptr;
+      o.a_lo = (const float*)jd.a.ptr_lo;
+      o.b_lo = (const float*)jd.b.ptr_lo;
+      o.c = jd.c_ptr;
+      o.a_max = jd.a.max_ptr;
+      o.b_max = jd.b.max_ptr;
+      o.a_exp = jd.a.exp_ptr;
+      o.b_exp = jd.b.exp_ptr;
+      o.c_exp = jd.c_exp;
+      o.c_max = jd.c_max;
+      o.a_shift = jd.a.leaf_shift;
+      o.b_shift = jd.b.leaf_shift;
+      o.mb = jd.mb;
+      o.nb = jd.nb;
+      o.kb = jd.kb;
+      o.natural = jd.c_natural;
+      std::memcpy(o.a_ktab, jd.a.ktab, sizeof(o.a_ktab));
+      std::memcpy(o.b_ktab, jd.b.ktab, sizeof(o.b_ktab));
+      o.a_outer = jd.a.r_outer;
+      o.b_outer = jd.b.r_outer;
+      o.a_k = jd.a.r_k;
+      o.b_k = jd.b.r_k;
+      o.inv_m = jd.r_inv_m;
+      o.inv_n = jd.r_inv_n;
+      const int64_t outs = pow2(jd.mb + jd.nb);
+      const int64_t tiles = (outs + togb::kOnceTile - 1) / togb::kOnceTile;
+      if ((int64_t)tf[i] + tiles > INT32_MAX / 2) return fail(TOGB_ERR_UNSUPPORTED, "slice-invariant phase too large to fuse");
+      tf[i + 1] = tf[i] + (int32_t)tiles;
+      for (int64_t t = 0; t < tiles; ++t) tj.push_back(i);
+      int w = 0;
+      for (int opnd : {J.left, J.right}) {
+        const Node& O = p->nodes[opnd];
+        if (O.leaf < 0) {
+          auto it = local.find(O.join);
+          if (it != local.end()) deps[2 * i + w] = it->second;
+        }
+        ++w;
+      }
+    }
+    off_j[g] = put(oj.data(), sizeof(togb::OnceJoin) * n);
+    off_tf[g] = put(tf.data(), sizeof(int32_t) * (n + 1));
+    off_dep[g] = put(deps.data(), sizeof(int32_t) * 2 * n);
+    off_tj[g] = put(tj.data(), sizeof(int32_t) * tj.size());
+    off_ctr[g] = ctr;
+    ctr += 1 + (size_t)n;
+    S.ol.n = n;
+    S.ol.total_tiles = tf[n];
+  }
+  if (img.empty()) {
+    p->once_segs_mode = mode;
+    return TOGB_OK;
+  }
+  char* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, img.size());
+  if (e != cudaSuccess) return cuda_fail(e, "fused slice-invariant tables");
+  p->once_bufs.push_back(d);
+  if ((e = cudaMemcpy(d, img.data(), img.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_fail(e, "fused slice-invariant tables");
+  if (ctr * 4 > p->once_ctr_bytes) {
+    uint32_t* c = nullptr;
+    if ((e = cudaMalloc(&c, ctr * 4)) != cudaSuccess) return cuda_fail(e, "fused slice-invariant counters");
+    p->once_bufs.push_back(c);
+    p->d_once_ctr = c;
+    p->once_ctr_bytes = ctr * 4;
+  }
+  for (size_t g = 0; g < G; ++g) {
+    OnceSeg& S = p->once_segs[g];
+    if (!S.fused) continue;
+    S.ol.joins = (const togb::OnceJoin*)(d + off_j[g]);
+    S.ol.tile_first = (const int32_t*)(d + off_tf[g]);
+    S.ol.deps = (const int32_t*)(d + off_dep[g]);
+    S.ol.tile_join = (const int32_t*)(d + off_tj[g]);
+    S.ol.counters = p->d_once_ctr + off_ctr[g];
+    S.ol.err = p->d_err;
+  }
+  p->once_segs_mode = mode;
+  return TOGB_OK;
+}
+
 // Queue one phase: the slice-invariant joins once (`once`, one slice per
 // launch), or the per-slice joins and the root reduction for a chunk of `nb`
 // slices.  With `ev`, event i is recorded before the phase's join i and one
@@ -629,6 +818,25 @@ togb_status enqueue_phase(togb_program* p, int mode, bool once, int nb, cudaStre
   const size_t mx_bytes = once ? p->max_once_bytes : p->max_bytes;
   if (mx_bytes) TOGB_CUDA(cudaMemsetAsync(mx, 0, mx_bytes, st));
   const int launch_slices = once ? 1 : nb;
+  if (once && !ev && p->once_segs_mode == mode && !p->once_segs.empty()) {
+    // Fused form of the slice-invariant phase (not while timing join by join).
+    if (p->once_ctr_bytes) TOGB_CUDA(cudaMemsetAsync(p->d_once_ctr, 0, p->once_ctr_bytes, st));
+    for (const OnceSeg& S : p->once_segs) {
+      cudaError_t e;
+      if (S.fused) {
+        e = togb::launch_once_list(mode, S.ol, st);
+      } else {
+        const int j = S.js[0];
+        const int kernel = join_kernel(p, p->nodes[p->joins[j]], mode);
+        if (kernel == togb::K_UMMA && mode == TOGB_MODE_SPLIT && p->use_tma[j])
+          e = togb::launch_umma(p->jds[j], &p->tmaps[2 * j], &p->tmaps[2 * j + 1], p->d_s0, 1, st);
+        else
+          e = togb::launch_join(mode, kernel, p->jds[j], p->d_s0, 1, st);
+      }
+      if (e != cudaSuccess) return cuda_fail(e, "join kernel launch");
+    }
+    return TOGB_OK;
+  }
   for (size_t i = 0; i < js.size(); ++i) {
     const int j = js[i];
     if (ev) TOGB_CUDA(cudaEventRecord((*ev)[i], st));
@@ -968,7 +1176,12 @@ togb_status togb_program_describe(togb_program* p, int mode, int32_t join, char*
   const Node& J = p->nodes[p->joins[join]];
   std::string s = "join " + std::to_string(join) + " mnk " + std::to_string(jd.mb) + " " + std::to_string(jd.nb) +
                   " " + std::to_string(jd.kb) + " kernel " + std::to_string(join_kernel(p, J, mode)) +
-                  " per_slice " + std::to_string(J.dep ? 1 : 0) + " c_natural " + std::to_string(jd.c_natural) + "\n";
+                  " per_slice " + std::to_string(J.dep ? 1 : 0) + " c_natural " + std::to_string(jd.c_natural);
+  if (join_kernel(p, J, mode) == togb::K_DIRECT) {
+    static const char* names[] = {"direct", "staged", "stream", "stream_kfast"};
+    s += std::string(" variant ") + names[togb::direct_variant(mode, jd)];
+  }
+  s += "\n";
   auto strides = [&](const char* name, const int64_t* v, int nb) {
     s += name;
     for (int i = 0; i < nb; ++i) s += " " + std::to_string(v[i]);
@@ -1113,8 +1326,10 @@ togb_status togb_program_run(togb_program* p, int mode, int64_t begin, int64_t e
     p->cur_ws = ws;
   }
   if (p->timing) p->join_ms.assign(p->joins.size(), 0.f);
+  togb_status r = prepare_once_fused(p, mode);
+  if (r != TOGB_OK) return r;
   // The slice-invariant joins first (once per call), then every chunk.
-  togb_status r = run_phase(p, mode, true, 1, st);
+  r = run_phase(p, mode, true, 1, st);
   for (int64_t s = begin; r == TOGB_OK && s < end; s += B) {
     const int nb = (int)std::min<int64_t>(B, end - s);
     cudaError_t e = togb::launch_set_s0(p->d_s0, s, st);
@@ -1160,6 +1375,7 @@ void togb_program_destroy(togb_program* p) {
   cudaFree(p->d_acc);
   cudaFree(p->d_s0);
   cudaFree(p->d_err);
+  for (void* b : p->once_bufs) cudaFree(b);
   if (p->own_ws) cudaFree(p->own_ws);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   delete p;
@@ -1241,6 +1457,8 @@ togb_status togb_batch_create(togb_program* const* progs, int32_t n, int mode, v
       p->cur_B = (int)B;
       p->cur_ws = ws;
     }
+    togb_status pr = prepare_once_fused(p, mode);
+    if (pr != TOGB_OK) { batch_free(b); return pr; }
     b->progs.push_back(p);
     b->ws.push_back(ws);
     b->B.push_back(B);
@@ -1401,6 +1619,8 @@ togb_status togb::static_contract_f64(const togb_program_desc* d, const double* 
   int64_t nvals = 0;
   togb_status r = lower_host(d, 0, &p, &nvals);
   if (r != TOGB_OK) return r;
+  p->allow_fused_once = false;  // the slice-invariant arena reuses memory: smallest scratch
+  plan_arena(p);
   const int64_t E = pow2(p->nodes[p->root].rank);
   const int64_t head = 256 + (2 * E * 8 + 255) / 256 * 256;
   const int64_t per = ws_per_slice(p, TOGB_MODE_F64);

@@ -5,8 +5,10 @@ leaf Y of at most 16 entries over k <= 2 shared edges.  The cases are chosen so
 that X's two lowest m bits are either its two lowest address bits or lie just
 above its k bits (the two operand layouts the streaming kernel reads), which
 the host-only lowering confirms without a GPU.  Sliced cases put the slice
-edges on Y and on X (per-slice X) or on Y alone (slice-invariant X, computed
-once and read by every slice).  Tolerances: 1e-12 (plain), 1e-6 (split),
+edges on Y and on X (per-slice X), on Y alone (slice-invariant X, computed
+once and read by every slice) or on X alone (slice-invariant leaf Y).  The
+same generator gives the short-K joins with large outputs that run on the
+staged kernel.  Tolerances: 1e-12 (plain), 1e-6 (split),
 relative to the largest entry."""
 import numpy as np
 import pytest
@@ -16,7 +18,10 @@ from tensororder_gb300 import runtime
 from tensororder_gb300.program import Leaf, Program
 
 
-def make_program(seed, m, k, n, slices=0, slice_x=True):
+def make_program(seed, m, k, n, slices=0, where="xy"):
+    """Slice edges on X's first leaf and on Y (``xy``), on Y only (``y``:
+    slice-invariant X, Y the product of two leaves sharing them) or on X only
+    (``x``: X's two leaves share them, Y a slice-invariant leaf)."""
     rng = np.random.default_rng(seed)
     fa = list(range(m))
     kk = list(range(m, m + k))
@@ -25,11 +30,13 @@ def make_program(seed, m, k, n, slices=0, slice_x=True):
     ya = [int(e) for e in rng.permutation(kk + fb)]
     cut = len(xa) // 2
     sl = [m + k + n + g for g in range(slices)]
-    if slice_x:
+    if where == "xy":
         leaves = [Leaf(xa[:cut] + sl, "dense"), Leaf(xa[cut:], "dense"), Leaf(ya + sl, "dense")]
         post = [0, 1, -1, 2, -1]
+    elif where == "x":
+        leaves = [Leaf(xa[:cut] + sl, "dense"), Leaf(xa[cut:] + sl, "dense"), Leaf(ya, "dense")]
+        post = [0, 1, -1, 2, -1]
     else:
-        # slice edges on Y only: Y is the product of two leaves sharing them
         half = len(ya) // 2
         leaves = [Leaf(xa[:cut], "dense"), Leaf(xa[cut:], "dense"), Leaf(ya[:half] + sl, "dense"),
                   Leaf(ya[half:] + sl, "dense")]
@@ -70,32 +77,59 @@ def stream_layout(prog, join):
     return None
 
 
-# (seed, m, k, n, slices, slice_x, layout)
+# (seed, m, k, n, slices, where, layout)
 CASES = [
-    (0, 12, 1, 2, 0, True, "mfast"), (13, 12, 1, 2, 0, True, "kfast"), (0, 13, 2, 1, 0, True, "mfast"),
-    (0, 12, 0, 4, 0, True, "mfast"), (1, 11, 2, 2, 0, True, "mfast"), (39, 11, 2, 2, 0, True, "kfast"),
-    (4, 14, 1, 3, 0, True, "kfast"), (2, 14, 1, 3, 0, True, "mfast"), (3, 10, 2, 0, 0, True, "mfast"),
-    (1, 12, 1, 2, 2, True, "mfast"), (32, 12, 1, 2, 2, True, "kfast"), (5, 13, 2, 1, 3, True, "mfast"),
-    (6, 14, 1, 3, 2, True, "kfast"), (2, 12, 0, 4, 2, True, "mfast"),
-    (0, 12, 1, 2, 3, False, "mfast"), (13, 12, 1, 2, 2, False, "kfast"), (4, 14, 1, 3, 3, False, "kfast"),
-    (1, 13, 2, 1, 2, False, "mfast"), (3, 12, 0, 4, 2, False, "mfast"),
+    (0, 12, 1, 2, 0, "xy", "mfast"), (13, 12, 1, 2, 0, "xy", "kfast"), (0, 13, 2, 1, 0, "xy", "mfast"),
+    (0, 12, 0, 4, 0, "xy", "mfast"), (1, 11, 2, 2, 0, "xy", "mfast"), (39, 11, 2, 2, 0, "xy", "kfast"),
+    (4, 14, 1, 3, 0, "xy", "kfast"), (2, 14, 1, 3, 0, "xy", "mfast"), (3, 10, 2, 0, 0, "xy", "mfast"),
+    (1, 12, 1, 2, 2, "xy", "mfast"), (32, 12, 1, 2, 2, "xy", "kfast"), (5, 13, 2, 1, 3, "xy", "mfast"),
+    (6, 14, 1, 3, 2, "xy", "kfast"), (2, 12, 0, 4, 2, "xy", "mfast"),
+    (0, 12, 1, 2, 3, "y", "mfast"), (13, 12, 1, 2, 2, "y", "kfast"), (4, 14, 1, 3, 3, "y", "kfast"),
+    (1, 13, 2, 1, 2, "y", "mfast"), (3, 12, 0, 4, 2, "y", "mfast"),
 ]
 
 
 def _prog(case):
-    seed, m, k, n, slices, slice_x, _ = case
-    return make_program(seed, m, k, n, slices, slice_x)
+    seed, m, k, n, slices, where, _ = case
+    return make_program(seed, m, k, n, slices, where)
 
 
 @pytest.mark.parametrize("case", CASES)
 def test_cases_have_the_streaming_layout(case):
-    """Host-only lowering: the root join of every case is a streaming join."""
+    """Host-only lowering: the root join of every case has a streaming layout,
+    and the library's own variant choice for it is the streaming kernel."""
     prog = _prog(case)
-    assert stream_layout(prog, prog.postorder.count(-1) - 1) == case[-1]
+    root = prog.postorder.count(-1) - 1
+    assert stream_layout(prog, root) == case[-1]
+    assert _variant(prog, root) == ("stream" if case[-1] == "mfast" else "stream_kfast")
+
+
+# Short-K joins whose output tiles reuse operand rows: the staged kernel,
+# including the orders that keep a slice-invariant operand's rows staged.
+STAGED = [
+    (0, 12, 2, 7, 2, "y", "staged"), (1, 12, 2, 7, 2, "x", "staged"), (2, 12, 2, 7, 2, "xy", "staged"),
+    (3, 9, 2, 9, 3, "y", "staged"), (4, 9, 2, 9, 2, "x", "staged"), (5, 11, 3, 5, 2, "x", "staged"),
+    (6, 8, 0, 8, 2, "y", "staged"), (7, 10, 1, 6, 0, "xy", "staged"),
+]
+
+
+def _variant(prog, join):
+    hp = runtime.HostProgram(prog)
+    try:
+        head = hp.describe(runtime.MODE_SPLIT, join).splitlines()[0].split()
+    finally:
+        hp.close()
+    return head[head.index("variant") + 1]
+
+
+@pytest.mark.parametrize("case", STAGED)
+def test_staged_cases_take_the_staged_kernel(case):
+    prog = _prog(case)
+    assert _variant(prog, prog.postorder.count(-1) - 1) == "staged"
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("case", CASES + STAGED)
 @pytest.mark.parametrize("mode,tol", [(runtime.MODE_F64, 1e-12), (runtime.MODE_SPLIT, 1e-6)])
 def test_stream_join(case, mode, tol, cuda):
     prog = _prog(case)
