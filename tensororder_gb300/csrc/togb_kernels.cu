@@ -234,8 +234,8 @@ struct StageInfo {
   int T, lm, ln;
   int slice_fast;       // tiles ordered slice-fastest in contiguous CTA ranges
   int a_inv, b_inv;     // the operand is the same for every slice
-  int a_row_bits[12];   // A s_outer index of the r-th staged m bit
-  int b_row_bits[12];
+  int a_row_bits[14];   // A s_outer index of the r-th staged m bit
+  int b_row_bits[14];
 };
 
 // One staged row of KK values from shared memory, in 16-byte (or 8-byte)
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
                                                             const __grid_constant__ StageInfo si,
                                                             const int64_t* __restrict__ d_s0, int nslices) {
   extern __shared__ __align__(16) unsigned char sm_dyn[];
-  __shared__ uint16_t IA[2][64], IB[2][64];
+  __shared__ uint16_t IA[3][64], IB[3][64];
   const int TB = si.T;
   const int rowsA = 1 << si.lm, rowsB = 1 << si.ln;
   // Dynamic shared memory: A rows, B rows, leaf residual rows, row offsets.
@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
   const uint64_t nmask = (1ull << jd.nb) - 1;
   const uint64_t lowmask = (1ull << TB) - 1;
   // Compaction tables: tile-local address q -> staged row of A and of B.
-  for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+  for (int i = threadIdx.x; i < 192; i += blockDim.x) {
     const int lvl = i >> 6, x = i & 63;
     const uint64_t q = ((uint64_t)x << (6 * lvl)) & lowmask;
     const uint64_t m = jd.c_natural ? (q >> jd.nb) : (uint64_t)dep(jd.r_inv_m, q);
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
   const int64_t s0 = d_s0 ? *d_s0 : 0;
   const int64_t tiles_per_slice = 1ll << (mnb - TB);
   const int64_t ntiles = (int64_t)nslices * tiles_per_slice;
-  const int per_thread = (1 << TB) / (4 * kThreads);  // vector groups per thread: 1, 2 or 4
+  const int per_thread = (1 << TB) / (4 * kThreads);  // vector groups per thread: 1 to 16
   int64_t t_begin, t_end, t_step;
   if (si.slice_fast) {
     const int64_t chunk = (ntiles + gridDim.x - 1) / gridDim.x;
@@ -337,15 +337,23 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
   }
   int64_t staged_pos = -1;  // tile position whose rows are staged
   int staged_b = -1;        // slice whose rows are staged
+  // Slice-fastest ranges step (pos, b) without a division per tile.
+  int64_t pos_f = si.slice_fast ? t_begin / nslices : 0;
+  int b_f = si.slice_fast ? (int)(t_begin - pos_f * nslices) : 0;
+  const int tps_bits = mnb - TB;
   for (int64_t t = t_begin; t < t_end; t += t_step) {
     int b;
     int64_t pos;
     if (si.slice_fast) {
-      pos = t / nslices;
-      b = (int)(t - pos * nslices);
+      pos = pos_f;
+      b = b_f;
+      if (++b_f == nslices) {
+        b_f = 0;
+        ++pos_f;
+      }
     } else {
-      b = (int)(t / tiles_per_slice);
-      pos = t - (int64_t)b * tiles_per_slice;
+      b = (int)(t >> tps_bits);
+      pos = t & (tiles_per_slice - 1);
     }
     if (MODE == 1 && b != carry_b) {  // block-uniform
       uint32_t v = carry;
@@ -406,8 +414,8 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
       const int q0 = 4 * (threadIdx.x + kThreads * i);
       // The row tables are OR-linear in the address bits: the two lowest
       // bits (j) contribute IA[0][j] / IB[0][j] to every group.
-      const int ra0 = IA[0][q0 & 63] | IA[1][(q0 >> 6) & 63];
-      const int rb0 = IB[0][q0 & 63] | IB[1][(q0 >> 6) & 63];
+      const int ra0 = IA[0][q0 & 63] | IA[1][(q0 >> 6) & 63] | IA[2][(q0 >> 12) & 63];
+      const int rb0 = IB[0][q0 & 63] | IB[1][(q0 >> 6) & 63] | IB[2][(q0 >> 12) & 63];
       T out[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
@@ -466,7 +474,8 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
 // contiguous, as N vectors.  The arithmetic order per output is dot_k's, so
 // the results equal k_direct's bit for bit.
 template <int KK, int NN, bool KFAST>
-__global__ void __launch_bounds__(kThreads) k_stream(const __grid_constant__ JoinDesc jd,
+__global__ void __launch_bounds__(kThreads, (KK * NN <= 4 || (KK * NN == 8 && KK >= 2)) ? 4 : (KK * NN == 8 ? 3 : 2))
+    k_stream(const __grid_constant__ JoinDesc jd,
                                                      const int64_t* __restrict__ d_s0, int nslices) {
   const int qb = jd.mb - 2;  // log2 of the quads of m per slice
   const int64_t quads = (int64_t)nslices << qb;
@@ -1316,39 +1325,51 @@ void staged_launch(Kern kern, const JoinDesc& jd, const StageInfo& si, const int
 }
 
 // The staged thread-per-output variant applies to K <= 16 when a tile of 2^T
-// (T in [10, 12]) output addresses touches at least 4 rows of each operand
+// (T in [10, 14]) output addresses touches at least 4 rows of each operand
 // (rows are reused) and the staged rows fit 64 KB.  Returns true when launched.
-bool staged_plan(int mode, const JoinDesc& jd, StageInfo& si, size_t& bytes) {
+// Tiles of 2^T output addresses, T in [10, 14]: the largest T whose launch
+// still has a tile for every resident CTA (about 152 x 8), else the smallest.
+bool staged_plan(int mode, const JoinDesc& jd, int nslices, StageInfo& si, size_t& bytes) {
   const int mnb = jd.mb + jd.nb;
   if (jd.kb > 4 || mnb < 10) return false;
   const int K = 1 << jd.kb;
   const size_t es = mode == 0 ? 8 : 4;
-  for (int T = mnb < 12 ? mnb : 12; T >= 10; --T) {
-    si = StageInfo{};
+  bool found = false;
+  StageInfo best{};
+  size_t best_bytes = 0;
+  for (int T = mnb < 14 ? mnb : 14; T >= 10; --T) {
+    StageInfo c{};
     int lm = 0, ln = 0;
     for (int i = 0; i < jd.mb; ++i)
-      if (jd.c_s_m[i] < (1ll << T)) si.a_row_bits[lm++] = i;
+      if (jd.c_s_m[i] < (1ll << T)) c.a_row_bits[lm++] = i;
     for (int i = 0; i < jd.nb; ++i)
-      if (jd.c_s_n[i] < (1ll << T)) si.b_row_bits[ln++] = i;
+      if (jd.c_s_n[i] < (1ll << T)) c.b_row_bits[ln++] = i;
     if (lm + ln != T || lm < 2 || ln < 2) continue;
-    bytes = ((size_t)1 << lm) * K * es + ((size_t)1 << ln) * K * es;
-    if (mode == 1) bytes += (jd.a.ptr_lo ? ((size_t)1 << lm) * K * 4 : 0) + (jd.b.ptr_lo ? ((size_t)1 << ln) * K * 4 : 0);
-    bytes += 4 * (((size_t)1 << lm) + ((size_t)1 << ln));  // row offsets
-    if (bytes > 64 * 1024) continue;
-    si.T = T;
-    si.lm = lm;
-    si.ln = ln;
-    si.a_inv = jd.a.batch_stride == 0 && jd.a.n_slice_terms == 0;
-    si.b_inv = jd.b.batch_stride == 0 && jd.b.n_slice_terms == 0;
-    return true;
+    size_t b = ((size_t)1 << lm) * K * es + ((size_t)1 << ln) * K * es;
+    if (mode == 1) b += (jd.a.ptr_lo ? ((size_t)1 << lm) * K * 4 : 0) + (jd.b.ptr_lo ? ((size_t)1 << ln) * K * 4 : 0);
+    b += 4 * (((size_t)1 << lm) + ((size_t)1 << ln));  // row offsets
+    if (b > 64 * 1024) continue;
+    c.T = T;
+    c.lm = lm;
+    c.ln = ln;
+    c.a_inv = jd.a.batch_stride == 0 && jd.a.n_slice_terms == 0;
+    c.b_inv = jd.b.batch_stride == 0 && jd.b.n_slice_terms == 0;
+    best = c;
+    best_bytes = b;
+    found = true;
+    if (((int64_t)nslices << (mnb - T)) >= 152 * 8) break;  // largest T with enough tiles
   }
-  return false;
+  if (found) {
+    si = best;
+    bytes = best_bytes;
+  }
+  return found;
 }
 
 bool launch_staged(int mode, const JoinDesc& jd, const int64_t* s0, int nslices, cudaStream_t st) {
   StageInfo si;
   size_t bytes = 0;
-  if (!staged_plan(mode, jd, si, bytes)) return false;
+  if (!staged_plan(mode, jd, nslices, si, bytes)) return false;
   si.slice_fast = nslices > 1 && (si.a_inv || si.b_inv);
   const int64_t tiles = (int64_t)nslices << (jd.mb + jd.nb - si.T);
 #define TOGB_STAGED(KK)                                                                                    \
@@ -1433,7 +1454,7 @@ int direct_variant(int mode, const JoinDesc& jd) {
   if (stream_ok(mode, jd, kfast)) return kfast ? 3 : 2;
   StageInfo si;
   size_t bytes = 0;
-  return staged_plan(mode, jd, si, bytes) ? 1 : 0;
+  return staged_plan(mode, jd, 1 << 20, si, bytes) ? 1 : 0;
 }
 
 cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t* s0, int nslices,

@@ -110,6 +110,8 @@ STAGED = [
     (0, 12, 2, 7, 2, "y", "staged"), (1, 12, 2, 7, 2, "x", "staged"), (2, 12, 2, 7, 2, "xy", "staged"),
     (3, 9, 2, 9, 3, "y", "staged"), (4, 9, 2, 9, 2, "x", "staged"), (5, 11, 3, 5, 2, "x", "staged"),
     (6, 8, 0, 8, 2, "y", "staged"), (7, 10, 1, 6, 0, "xy", "staged"),
+    # 64 slices: enough tiles for the 2^13 / 2^14-address tiles
+    (8, 12, 2, 7, 6, "y", "staged"), (9, 9, 2, 9, 6, "x", "staged"), (10, 11, 3, 5, 6, "xy", "staged"),
 ]
 
 
