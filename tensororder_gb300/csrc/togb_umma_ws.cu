@@ -238,8 +238,13 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
         const unsigned char* raw = smem + rs * L::RAW;
         unsigned char* hi = smem + NR * L::RAW + cs * L::CONV;
         unsigned char* lo = hi + L::RAW;
+        // 16-byte pieces of a row the chunk's MMA k-steps read (two per k-step
+        // of 8); the rest (K past the end) is neither read nor converted.
+        const int live = 2 * min(4, ksteps - 4 * c);
 #pragma unroll 4
         for (int e = ct; e < L::RAW / 16; e += kConv) {
+          // 128-byte swizzle: piece p of row r holds logical piece p ^ (r % 8)
+          if (live < 8 && (((e & 7) ^ ((e >> 3) & 7)) >= live)) continue;
           const float4 x = *reinterpret_cast<const float4*>(raw + e * 16);
           float4 h, l;
           split4(x, e * 16 < L::A_BYTES ? fa : fb, h, l);
