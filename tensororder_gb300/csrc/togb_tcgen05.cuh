@@ -34,6 +34,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
 
 // Bounded wait for phase `parity` of the mbarrier at `addr`.
 __device__ bool mbar_wait_bounded(uint32_t addr, uint32_t parity) {
+  if (mbar_try_wait(addr, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_wait(addr, parity))
     if (clock64() - t0 > kWaitCycles) return false;
@@ -146,6 +147,7 @@ __device__ __forceinline__ void mbar_arrive(uint32_t addr) {
 // `*abort` (a shared flag): every role of a warp-specialised kernel leaves
 // within about a second of the first expired wait.
 __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t addr, uint32_t parity, volatile int* abort) {
+  if (mbar_try_wait(addr, parity)) return true;  // the common case: no clock read
   const long long t0 = clock64();
   while (!mbar_try_wait(addr, parity)) {
     if (*abort) return false;

@@ -103,7 +103,11 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
   constexpr uint32_t kCols = 512;      // all of tensor memory (one CTA per SM)
   constexpr int NSETS = kCols / BN;    // accumulator sets in rotation
   constexpr int kConv = 192;          // converter threads (warps 2-7)
-  constexpr int kRead = 256;          // read-out threads
+  // Consumer barriers count warps: one elected lane arrives for its warp
+  // after a __syncwarp, so a stage costs 6 (or 8) arrivals instead of one per
+  // thread.
+  constexpr int kConvWarps = kConv / 32;
+  constexpr int kReadWarps = 8;
   extern __shared__ unsigned char dyn_raw[];
   __shared__ __align__(8) uint64_t full[NR], rawfree[NR], conv[NC], cfree[NC], accf[NSETS], acce[NSETS], fin;
   __shared__ uint32_t tmem_sh;
@@ -125,15 +129,15 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
   if (tid == 0) {
     for (int i = 0; i < NR; ++i) {
       mbar_init(smem_u32(&full[i]), 1);
-      mbar_init(smem_u32(&rawfree[i]), kConv);
+      mbar_init(smem_u32(&rawfree[i]), kConvWarps);
     }
     for (int i = 0; i < NC; ++i) {
-      mbar_init(smem_u32(&conv[i]), kConv);
+      mbar_init(smem_u32(&conv[i]), kConvWarps);
       mbar_init(smem_u32(&cfree[i]), 1);
     }
     for (int i = 0; i < NSETS; ++i) {
       mbar_init(smem_u32(&accf[i]), 1);
-      mbar_init(smem_u32(&acce[i]), kRead);
+      mbar_init(smem_u32(&acce[i]), kReadWarps);
     }
     mbar_init(smem_u32(&fin), 1);
     fence_mbar_init();
@@ -197,14 +201,22 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
             tc_fence_after();
             const uint32_t d = tmem + (uint32_t)(set * BN);
             const int t0 = 2 * h, t1 = min(2 * h + 2, ksteps - 4 * c);
-            uint32_t accum = 0;
-            for (int k = t0; k < t1; ++k) {  // corrections while the set is small
-              umma_tf32(d, smem_desc_sw128(a_hi + 32 * k), smem_desc_sw128(b_lo + 32 * k), idesc, accum);
-              accum = 1;
-              umma_tf32(d, smem_desc_sw128(a_lo + 32 * k), smem_desc_sw128(b_hi + 32 * k), idesc, 1u);
+            // Descriptors of the window's first k-step; a k-step of 8 FP32
+            // values is 32 bytes, +2 in the descriptor's 16-byte address field.
+            const uint64_t dah = smem_desc_sw128(a_hi + 32 * t0), dal = smem_desc_sw128(a_lo + 32 * t0);
+            const uint64_t dbh = smem_desc_sw128(b_hi + 32 * t0), dbl = smem_desc_sw128(b_lo + 32 * t0);
+            if (t1 - t0 == 2) {  // full window: six MMAs, corrections first while the set is small
+              umma_tf32(d, dah, dbl, idesc, 0u);
+              umma_tf32(d, dal, dbh, idesc, 1u);
+              umma_tf32(d, dah + 2, dbl + 2, idesc, 1u);
+              umma_tf32(d, dal + 2, dbh + 2, idesc, 1u);
+              umma_tf32(d, dah, dbh, idesc, 1u);
+              umma_tf32(d, dah + 2, dbh + 2, idesc, 1u);
+            } else {  // one k-step (K = 8 or an odd tail)
+              umma_tf32(d, dah, dbl, idesc, 0u);
+              umma_tf32(d, dal, dbh, idesc, 1u);
+              umma_tf32(d, dah, dbh, idesc, 1u);
             }
-            for (int k = t0; k < t1; ++k)
-              umma_tf32(d, smem_desc_sw128(a_hi + 32 * k), smem_desc_sw128(b_hi + 32 * k), idesc, 1u);
             umma_commit(smem_u32(&accf[set]));
             ++gw;
           }
@@ -229,8 +241,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
       const float fa = pow2f(op_shift(jd.a, b)), fb = pow2f(op_shift(jd.b, b));
       for (int c = 0; c < nchunks; ++c, ++gc) {
         const int rs = gc % NR, ru = gc / NR, cs = gc % NC, cu = gc / NC;
-        if (!mbar_wait_or_abort(smem_u32(&full[rs]), ru & 1, abort) ||
-            (gc >= NC && !mbar_wait_or_abort(smem_u32(&cfree[cs]), (cu - 1) & 1, abort))) {
+        const bool got = mbar_wait_or_abort(smem_u32(&full[rs]), ru & 1, abort) &&
+                         (gc < NC || mbar_wait_or_abort(smem_u32(&cfree[cs]), (cu - 1) & 1, abort));
+        if (!__all_sync(0xffffffffu, got)) {  // warp-uniform exit
           *abort = 1;
           ok = false;
           break;
@@ -251,9 +264,11 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
           *reinterpret_cast<float4*>(hi + e * 16) = h;
           *reinterpret_cast<float4*>(lo + e * 16) = l;
         }
-        mbar_arrive(smem_u32(&rawfree[rs]));  // raw stage read: the next load may land there
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&rawfree[rs]));  // raw stage read: the next load may land there
         fence_async_smem();
-        mbar_arrive(smem_u32(&conv[cs]));
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&conv[cs]));
       }
     }
   } else if (warp >= 8) {
@@ -282,8 +297,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
         for (int w = 0; w < nwin;) {
           const bool two = w + 1 < nwin;
           const int set0 = gw % NSETS, set1 = (gw + 1) % NSETS;
-          if (!mbar_wait_or_abort(smem_u32(&accf[set0]), (gw / NSETS) & 1, abort) ||
-              (two && !mbar_wait_or_abort(smem_u32(&accf[set1]), ((gw + 1) / NSETS) & 1, abort))) {
+          const bool got = mbar_wait_or_abort(smem_u32(&accf[set0]), (gw / NSETS) & 1, abort) &&
+                           (!two || mbar_wait_or_abort(smem_u32(&accf[set1]), ((gw + 1) / NSETS) & 1, abort));
+          if (!__all_sync(0xffffffffu, got)) {
             *abort = 1;
             break;
           }
@@ -298,15 +314,18 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
             for (int j = 0; j < 16; ++j) acc[col + j] += two ? v0[j] + v1[j] : v0[j];
           }
           tc_fence_before();
-          mbar_arrive(smem_u32(&acce[set0]));
-          if (two) mbar_arrive(smem_u32(&acce[set1]));
+          __syncwarp();
+          if (lane == 0) {
+            mbar_arrive(smem_u32(&acce[set0]));
+            if (two) mbar_arrive(smem_u32(&acce[set1]));
+          }
           w += two ? 2 : 1;
           gw += two ? 2 : 1;
         }
       } else {
         for (int w = 0; w < nwin; ++w, ++gw) {
           const int set = gw % NSETS;
-          if (!mbar_wait_or_abort(smem_u32(&accf[set]), (gw / NSETS) & 1, abort)) {
+          if (!__all_sync(0xffffffffu, mbar_wait_or_abort(smem_u32(&accf[set]), (gw / NSETS) & 1, abort))) {
             *abort = 1;
             break;
           }
@@ -324,10 +343,11 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
             }
           }
           tc_fence_before();
-          mbar_arrive(smem_u32(&acce[set]));
+          __syncwarp();
+          if (lane == 0) mbar_arrive(smem_u32(&acce[set]));
         }
       }
-      if (*abort) break;
+      if (__any_sync(0xffffffffu, *abort != 0)) break;  // warp-uniform
       const int mlim = (int)min((int64_t)kBM, M - (int64_t)m0);
       const int nlim = (int)min((int64_t)BN, N - (int64_t)n0);
       float* __restrict__ C = (float*)jd.c_ptr + (int64_t)b * jd.c_batch_stride + deposit(jd.c_s_m, m0) +
