@@ -260,6 +260,7 @@ def main():
     with ClockSampler(local) as clocks:
         split_ms, split_val = timed(runtime.MODE_SPLIT, ws_split, args.steps, args.warmup)
     torch.cuda.synchronize(dev)
+    launches_per_count = dp.launch_count(runtime.MODE_SPLIT)  # as the timed steps queued them
     t_split = float(np.sum(split_ms)) / 1e3
     if world > 1:
         t = torch.tensor([t_split], device=dev)
@@ -318,8 +319,8 @@ def main():
                  "algorithmic_bytes": top_bytes, "traffic": None})
     if (mb, nb, kb, kern) == (8, 11, 9, 3):
         # DRAM read + write of this join in an ncu capture (--set full) of its
-        # first 32 slices, 151.1 + 36.6 MB, scaled to the slices of one launch.
-        roof["traffic"] = (151.133184e6 + 36.597504e6) * runs / 32
+        # first 32 slices, 151.1 + 39.4 MB, scaled to the slices of one launch.
+        roof["traffic"] = (151.11168e6 + 39.404544e6) * runs / 32
         roof["traffic_source"] = "ncu capture of 32 slices scaled by %d/32" % runs
 
     # End to end through the plugin's public call: host program in, count out.
@@ -372,8 +373,9 @@ def main():
         "e2e": {"value": 1e3 / float(np.mean(e2e_ms)), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "path": "GB300SplitAPI.contract_program(host program) -> libtogb C ABI"},
-        # per count: the slice-invariant joins, the slice base, the per-slice joins and the root
-        "gpu_launches": (int(info.num_launches) + 1 + int(info.num_joins_once)) * args.steps,
+        # per count: the fused slice-invariant lists and other slice-invariant joins, then per
+        # chunk the slice base, the per-slice joins and the root
+        "gpu_launches": launches_per_count * args.steps,
     }
     if not args.no_batch:
         line["batch512"] = batch_line(args, dev)

@@ -150,6 +150,14 @@ togb_status togb_program_result(togb_program* prog, void* stream, double* out, d
  * for every slice or 0 when it runs once per call.  n = num_joins. */
 togb_status togb_program_joins(const togb_program* prog, int mode, int32_t* out, int32_t n);
 
+/* Kernel launches of one count in `mode` with the descriptors of the last
+ * togb_program_run: the slice-invariant phase (one per fused list of
+ * thread-per-output joins and one per other join), then per chunk of slices
+ * the slice-base update, every per-slice join and the root reduction.  Before
+ * any run, the unfused count of a single chunk.  No counterpart in the
+ * reference. */
+togb_status togb_program_launch_count(const togb_program* prog, int mode, int64_t* launches);
+
 /* Choose the kernel of join `join` in `mode` (kernel ids as in
  * togb_program_joins; -1 restores the default).  A kernel that cannot run the
  * join in that form -- the split form's leaf residuals are applied only by the

@@ -1245,6 +1245,17 @@ togb_status togb_program_joins(const togb_program* p, int mode, int32_t* out, in
   return TOGB_OK;
 }
 
+togb_status togb_program_launch_count(const togb_program* p, int mode, int64_t* launches) {
+  if (!p || !launches) return fail(TOGB_ERR_INVALID, "null argument");
+  if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
+  const bool fused = p->once_segs_mode == mode && !p->once_segs.empty();
+  const int64_t once = fused ? (int64_t)p->once_segs.size() : (int64_t)p->once.size();
+  const int64_t B = p->cur_mode == mode && p->cur_B > 0 ? p->cur_B : p->num_slices;
+  const int64_t chunks = (p->num_slices + B - 1) / B;
+  *launches = once + chunks * ((int64_t)p->per.size() + 2);
+  return TOGB_OK;
+}
+
 togb_status togb_program_set_kernel(togb_program* p, int mode, int32_t join, int32_t kernel) {
   if (!p) return fail(TOGB_ERR_INVALID, "null program");
   if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");

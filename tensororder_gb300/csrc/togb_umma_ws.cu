@@ -17,12 +17,12 @@
 //   warps 8-15    read-out: drain the tensor-memory accumulators into FP32
 //                 registers and run the epilogue.
 // The tensor core truncates its FP32 accumulation, so one accumulator must not
-// see many large updates.  The K range is therefore cut into windows of 16
-// (two MMA k-steps); each window accumulates into a fresh tensor-memory set
-// (512 / BN sets used in rotation, so the MMAs run several windows ahead of
-// the read-out), correction products first while the set is still small, main
-// products last, and the read-out warps add the window into round-to-nearest
-// registers while later windows' MMAs run.
+// see many large updates.  The K range is therefore cut into windows of 32
+// (one TMA chunk, four MMA k-steps); each window accumulates into a fresh
+// tensor-memory set (512 / BN sets used in rotation, so the MMAs run several
+// windows ahead of the read-out), correction products first while the set is
+// still small, main products last, and the read-out warps add the window into
+// round-to-nearest registers while later windows' MMAs run.
 //
 // The kernel is persistent (one CTA per SM walking the tiles), so the next
 // tile's loads, conversions and first MMAs overlap the current tile's
@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
   const uint32_t sbase = smem_u32(smem);
   const int64_t M = 1ll << jd.mb, N = 1ll << jd.nb, K = 1ll << jd.kb;
   const int ksteps = K >= 8 ? (int)(K / 8) : 1;  // MMA k-steps of 8
-  const int nwin = (ksteps + 1) / 2;              // windows of two k-steps
-  const int nchunks = (nwin + 1) / 2;             // TMA chunks of four k-steps
+  const int nchunks = (ksteps + 3) / 4;           // TMA chunks of four k-steps
+  const int nwin = nchunks;                       // one accumulation window per chunk
 
   for (int i = tid; i < kBM; i += kWsThreads) tCm[i] = (int32_t)deposit(jd.c_s_m, i);
   for (int i = tid; i < BN; i += kWsThreads) tCn[i] = (int32_t)deposit(jd.c_s_n, i);
@@ -191,8 +191,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
           tc_fence_after();
           const uint32_t a_hi = sbase + NR * L::RAW + st * L::CONV, b_hi = a_hi + L::A_BYTES;
           const uint32_t a_lo = a_hi + L::RAW, b_lo = a_lo + L::A_BYTES;
-          for (int h = 0; h < 2; ++h) {
-            if (2 * c + h >= nwin) break;
+          {
             const int set = gw % NSETS;
             if (gw >= NSETS && !mbar_wait_or_abort(smem_u32(&acce[set]), (gw / NSETS - 1) & 1, abort)) {
               ok = false;
@@ -200,22 +199,25 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
             }
             tc_fence_after();
             const uint32_t d = tmem + (uint32_t)(set * BN);
-            const int t0 = 2 * h, t1 = min(2 * h + 2, ksteps - 4 * c);
-            // Descriptors of the window's first k-step; a k-step of 8 FP32
+            const int ks = min(4, ksteps - 4 * c);  // k-steps in this chunk
+            // Descriptors of the chunk's first k-step; a k-step of 8 FP32
             // values is 32 bytes, +2 in the descriptor's 16-byte address field.
-            const uint64_t dah = smem_desc_sw128(a_hi + 32 * t0), dal = smem_desc_sw128(a_lo + 32 * t0);
-            const uint64_t dbh = smem_desc_sw128(b_hi + 32 * t0), dbl = smem_desc_sw128(b_lo + 32 * t0);
-            if (t1 - t0 == 2) {  // full window: six MMAs, corrections first while the set is small
-              umma_tf32(d, dah, dbl, idesc, 0u);
-              umma_tf32(d, dal, dbh, idesc, 1u);
-              umma_tf32(d, dah + 2, dbl + 2, idesc, 1u);
-              umma_tf32(d, dal + 2, dbh + 2, idesc, 1u);
-              umma_tf32(d, dah, dbh, idesc, 1u);
-              umma_tf32(d, dah + 2, dbh + 2, idesc, 1u);
-            } else {  // one k-step (K = 8 or an odd tail)
-              umma_tf32(d, dah, dbl, idesc, 0u);
-              umma_tf32(d, dal, dbh, idesc, 1u);
-              umma_tf32(d, dah, dbh, idesc, 1u);
+            const uint64_t dah = smem_desc_sw128(a_hi), dal = smem_desc_sw128(a_lo);
+            const uint64_t dbh = smem_desc_sw128(b_hi), dbl = smem_desc_sw128(b_lo);
+            if (ks == 4) {  // full chunk: twelve MMAs, corrections first while the set is small
+#pragma unroll
+              for (int k = 0; k < 4; ++k) {
+                umma_tf32(d, dah + 2 * k, dbl + 2 * k, idesc, k ? 1u : 0u);
+                umma_tf32(d, dal + 2 * k, dbh + 2 * k, idesc, 1u);
+              }
+#pragma unroll
+              for (int k = 0; k < 4; ++k) umma_tf32(d, dah + 2 * k, dbh + 2 * k, idesc, 1u);
+            } else {  // short K or the tail chunk
+              for (int k = 0; k < ks; ++k) {
+                umma_tf32(d, dah + 2 * k, dbl + 2 * k, idesc, k ? 1u : 0u);
+                umma_tf32(d, dal + 2 * k, dbh + 2 * k, idesc, 1u);
+              }
+              for (int k = 0; k < ks; ++k) umma_tf32(d, dah + 2 * k, dbh + 2 * k, idesc, 1u);
             }
             umma_commit(smem_u32(&accf[set]));
             ++gw;
@@ -433,7 +435,7 @@ int umma_ws_box_rows_b(int nb) { return nb >= 7 ? 128 : 64; }
 
 cudaError_t launch_umma_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorMap& tb, int nslices,
                            cudaStream_t st) {
-  // More than 64 windows of 16 (K > 1024): the paired read-out.
+  // More than 32 windows of 32 (K > 1024): the paired read-out.
   const bool pairs = jd.kb > 10;
   if (jd.nb >= 7)
     return pairs ? launch_ws<128, 2, 2, true>(jd, ta, tb, nslices, st) : launch_ws<128, 2, 2, false>(jd, ta, tb, nslices, st);

@@ -93,6 +93,7 @@ EXPORTS = [
     "togb_mlp_param_count", "togb_mlp_scratch_floats", "togb_mlp_forward", "togb_mlp_loss_grad", "togb_mlp_adam",
     "togb_batch_create", "togb_batch_run", "togb_batch_results", "togb_batch_destroy",
     "togb_program_create_host", "togb_program_describe", "togb_program_create_compact",
+    "togb_program_launch_count",
 ]
 
 KERNEL_NAMES = {0: "direct", 1: "tiled", 2: "reduce", 3: "tensor"}
@@ -130,6 +131,7 @@ def lib():
     L.togb_probe_peak.argtypes = [ctypes.c_int, c_void, ctypes.POINTER(ctypes.c_double)]
     L.togb_contract_static_f64.argtypes = [ctypes.POINTER(ProgramDesc), c_void, c_void, c_void]
     L.togb_program_joins.argtypes = [c_void, ctypes.c_int, _i32p, ctypes.c_int32]
+    L.togb_program_launch_count.argtypes = [c_void, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
     L.togb_program_set_kernel.argtypes = [c_void, ctypes.c_int, ctypes.c_int32, ctypes.c_int32]
     L.togb_program_kernel_allowed.argtypes = [c_void, ctypes.c_int, ctypes.c_int32, ctypes.c_int32, _i32p]
     L.togb_batch_create.argtypes = [ctypes.POINTER(c_void), ctypes.c_int32, ctypes.c_int, ctypes.POINTER(c_void),
@@ -354,6 +356,12 @@ class DeviceProgram:
         out = np.zeros((max(n, 1), 5), dtype=np.int32)
         check(lib().togb_program_joins(self._h, int(mode), out.ctypes.data_as(_i32p), n))
         return out[:n]
+
+    def launch_count(self, mode):
+        """Kernel launches of one count in ``mode`` as the last run queued them."""
+        out = ctypes.c_int64()
+        check(lib().togb_program_launch_count(self._h, int(mode), ctypes.byref(out)))
+        return int(out.value)
 
     def set_kernel(self, mode, join, kernel):
         """Run ``join`` with ``kernel`` (an id of ``KERNEL_NAMES``; -1 = default) in ``mode``."""
