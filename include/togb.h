@@ -154,8 +154,8 @@ togb_status togb_program_joins(const togb_program* prog, int mode, int32_t* out,
  * togb_program_run: the slice-invariant phase (one per fused list of
  * thread-per-output joins and one per other join), then per chunk of slices
  * the slice-base update, every per-slice join and the root reduction.  Before
- * any run, the unfused count of a single chunk.  No counterpart in the
- * reference. */
+ * any run (and for host-only programs) the phase as a run would queue it, with
+ * all slices in one chunk.  No counterpart in the reference. */
 togb_status togb_program_launch_count(const togb_program* prog, int mode, int64_t* launches);
 
 /* Choose the kernel of join `join` in `mode` (kernel ids as in

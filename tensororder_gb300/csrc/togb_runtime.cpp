@@ -648,20 +648,16 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
 // copies each list's tables to the device.  Tables of earlier builds stay
 // allocated until the program is destroyed: a batch graph captured from them
 // may still be launched.
-togb_status prepare_once_fused(togb_program* p, int mode) {
-  if (p->once_segs_mode == mode) return TOGB_OK;
-  p->once_segs.clear();
-  p->once_segs_mode = -1;
-  if (!p->once_no_reuse || p->once.empty()) {
-    p->once_segs_mode = mode;
-    return TOGB_OK;
-  }
-  // Every join as early as its producers allow, in the order F0 N0 F1 N1 ...
-  // (F: fused lists of thread-per-output joins, N: the other joins, one
-  // launch each).  A thread-per-output join goes to the first F after all of
-  // its producers, any other join to the first N after them.  Inside an F the
-  // joins are ordered by depth, so a claimed tile waits only for joins whose
-  // tiles were claimed (and mostly finished) well before it.
+// The steps of the slice-invariant phase in `mode`: fused lists of
+// thread-per-output joins and single launches of the other joins.  Every join
+// goes as early as its producers allow, in the order F0 N0 F1 N1 ... (F: fused
+// lists, N: the other joins, one launch each).  A thread-per-output join goes
+// to the first F after all of its producers, any other join to the first N
+// after them.  Inside an F the joins are ordered by depth, so a claimed tile
+// waits only for joins whose tiles were claimed (and mostly finished) well
+// before it.  Host-only: the device tables are built by prepare_once_fused.
+std::vector<OnceSeg> once_segments(const togb_program* p, int mode) {
+  std::vector<OnceSeg> segs;
   std::unordered_map<int, int> place, depth;  // join -> step index (F_s = 2s, N_t = 2t + 1), depth in its F
   int steps = 0;
   for (int j : p->once) {
@@ -690,17 +686,29 @@ togb_status prepare_once_fused(togb_program* p, int mode) {
     if (members.empty()) continue;
     std::stable_sort(members.begin(), members.end());
     if (st % 2 == 0) {
-      p->once_segs.emplace_back();
-      p->once_segs.back().fused = true;
-      for (auto& m : members) p->once_segs.back().js.push_back(p->once[m.second]);
+      segs.emplace_back();
+      segs.back().fused = true;
+      for (auto& m : members) segs.back().js.push_back(p->once[m.second]);
     } else {
       for (auto& m : members) {
-        p->once_segs.emplace_back();
-        p->once_segs.back().fused = false;
-        p->once_segs.back().js.push_back(p->once[m.second]);
+        segs.emplace_back();
+        segs.back().fused = false;
+        segs.back().js.push_back(p->once[m.second]);
       }
     }
   }
+  return segs;
+}
+
+togb_status prepare_once_fused(togb_program* p, int mode) {
+  if (p->once_segs_mode == mode) return TOGB_OK;
+  p->once_segs.clear();
+  p->once_segs_mode = -1;
+  if (!p->once_no_reuse || p->once.empty()) {
+    p->once_segs_mode = mode;
+    return TOGB_OK;
+  }
+  p->once_segs = once_segments(p, mode);
   // Host images of the tables: [OnceJoin x n][tile_first x (n + 1)][deps x 2n][tile_join x tiles],
   // 256-byte aligned pieces.
   std::vector<char> img;
@@ -1248,8 +1256,12 @@ togb_status togb_program_joins(const togb_program* p, int mode, int32_t* out, in
 togb_status togb_program_launch_count(const togb_program* p, int mode, int64_t* launches) {
   if (!p || !launches) return fail(TOGB_ERR_INVALID, "null argument");
   if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
-  const bool fused = p->once_segs_mode == mode && !p->once_segs.empty();
-  const int64_t once = fused ? (int64_t)p->once_segs.size() : (int64_t)p->once.size();
+  int64_t once = (int64_t)p->once.size();
+  if (p->once_segs_mode == mode) {
+    if (!p->once_segs.empty()) once = (int64_t)p->once_segs.size();
+  } else if (p->once_no_reuse && !p->once.empty()) {
+    once = (int64_t)once_segments(p, mode).size();  // as a run in this form would queue them
+  }
   const int64_t B = p->cur_mode == mode && p->cur_B > 0 ? p->cur_B : p->num_slices;
   const int64_t chunks = (p->num_slices + B - 1) / B;
   *launches = once + chunks * ((int64_t)p->per.size() + 2);

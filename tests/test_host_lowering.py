@@ -1,0 +1,49 @@
+"""Host-only lowering (no GPU): the launch plan of a count.
+
+The slice-invariant joins of a program run as fused lists of thread-per-output
+joins plus single launches of the other joins; a count is that phase, then per
+chunk of slices the slice-base update, every per-slice join and the root
+reduction.  `togb_program_launch_count` of a host-only program gives the plan a
+run would queue with every slice in one chunk."""
+import ctypes
+import gzip
+import json
+import os
+
+import pytest
+
+from conftest import ROOT, golden_names, load_golden
+from tensororder_gb300 import runtime
+from tensororder_gb300.program import Program
+
+
+def launch_plan(prog, mode):
+    hp = runtime.HostProgram(prog)
+    try:
+        out = ctypes.c_int64()
+        runtime.check(runtime.lib().togb_program_launch_count(hp._h, int(mode), ctypes.byref(out)))
+        return out.value, int(hp.info.num_joins_once), int(hp.info.num_launches)
+    finally:
+        hp.close()
+
+
+@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("mode", [runtime.MODE_F64, runtime.MODE_SPLIT])
+def test_launch_count_of_golden_plans(name, mode):
+    prog = Program.from_dict(load_golden(name)["program"])
+    launches, once, per_and_root = launch_plan(prog, mode)
+    per_chunk = per_and_root + 1  # slice base, per-slice joins, root
+    if once == 0:
+        assert launches == per_chunk
+    else:
+        assert 1 <= launches - per_chunk <= min(once, 4)
+
+
+@pytest.mark.parametrize("mode", [runtime.MODE_F64, runtime.MODE_SPLIT])
+def test_n220_slice_invariant_phase_is_two_launches(mode):
+    """360 thread-per-output joins in one fused list and one GEMM-shaped join."""
+    with gzip.open(os.path.join(ROOT, "tensororder_gb300", "plans", "wvc220_s10.json.gz"), "rt") as f:
+        prog = Program.from_dict(json.load(f)["program"])
+    launches, once, per_and_root = launch_plan(prog, mode)
+    assert once == 361
+    assert launches == 2 + per_and_root + 1
