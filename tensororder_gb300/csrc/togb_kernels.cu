@@ -1,19 +1,25 @@
 // CUDA kernels of the contraction path (sm_103a).
 //
-// Two join kernels cover every pairwise contraction of binary-index tensors:
+// The CUDA-core join kernels (the tensor-core GEMM joins are in togb_umma_ws.cu
+// and togb_umma.cu) cover every pairwise contraction of binary-index tensors:
 //
 //  * k_direct -- one thread per output entry, a K-long dot product with
 //    deposit addressing.  Used when one GEMM extent is small (outer products,
-//    matrix-vector shapes, the tiny joins that dominate the join count).
+//    matrix-vector shapes, the tiny joins that dominate the join count).  Two
+//    variants take over when the shapes allow, with the same arithmetic per
+//    output: k_direct_staged (short K, operand rows staged per output tile)
+//    and k_stream (a long operand against a tiny one, 16-byte vectors).
 //  * k_tiled  -- 64x64x16 shared-memory tiled GEMM, 4x4 register blocking.
 //    Tiles are gathered through per-CTA offset tables, so any axis
 //    permutation of either operand is read in place (no transpose pass).
 //  * k_reduce -- one CTA per (slice, output entry) for joins with a few
 //    outputs and a long K (the root of a tree is a 1x1xK dot product): strided
 //    per-thread partial sums (compensated in the split form), then a pairwise
-//    tree across the CTA.
+//    tree across the CTA.  k_reduce_vec reads contiguous K runs as vectors.
+//  * k_once_list -- one launch for a list of slice-invariant thread-per-output
+//    joins, CTAs claiming output tiles in dependency order.
 //
-// Both are templated on the form:
+// They are templated on the form:
 //  * MODE 0 (FP64): FP64 storage and FMA.
 //  * MODE 1 (split): FP32 storage; each (tensor, slice) carries a
 //    power-of-two exponent.  Inputs are normalised on load so that their
