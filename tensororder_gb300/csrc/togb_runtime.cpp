@@ -186,6 +186,7 @@ struct togb_program {
   size_t once_ctr_bytes = 0;
   std::vector<void*> once_bufs;     // device copies of the segments' tables (freed with the program)
   std::map<int, cudaGraphExec_t> graphs;  // by chunk slice count
+  std::map<int, int> phase_runs;          // launches of each phase key since the last clear
   bool use_graphs = true;
   bool timing = false;
   bool host_only = false;  // lowered for inspection only; owns no device memory
@@ -220,6 +221,7 @@ int64_t ws_fixed(const togb_program* p, int mode) { return kWsSlack + ws_once(p,
 void clear_graphs(togb_program* p) {
   for (auto& kv : p->graphs) cudaGraphExecDestroy(kv.second);
   p->graphs.clear();
+  p->phase_runs.clear();
 }
 
 // Bottom-up part of a join's plan: edge sets, reference output order, kernel,
@@ -892,6 +894,10 @@ togb_status run_phase(togb_program* p, int mode, bool once, int nb, cudaStream_t
   if (!p->use_graphs) return enqueue_phase(p, mode, once, nb, st, nullptr);
   const int key = once ? -1 : nb;
   auto it = p->graphs.find(key);
+  // A phase's first run is queued launch by launch: a program contracted once
+  // (the plugin's contract_sliced call) pays no capture or instantiation.
+  // From the second run on it is captured once and replayed.
+  if (it == p->graphs.end() && p->phase_runs[key]++ == 0) return enqueue_phase(p, mode, once, nb, st, nullptr);
   if (it == p->graphs.end()) {
     cudaGraph_t g = nullptr;
     TOGB_CUDA(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
