@@ -171,6 +171,17 @@ togb_status togb_program_set_kernel(togb_program* prog, int mode, int32_t join, 
 togb_status togb_program_kernel_allowed(const togb_program* prog, int mode, int32_t join, int32_t kernel,
                                         int32_t* allowed);
 
+/* Limit, in SM clock cycles, of every device-side wait of this program's
+ * kernels: a fused slice-invariant list waiting for a producer tile published
+ * by another CTA of the same launch, and the tensor-core joins' load / MMA /
+ * read-out pipeline waits.  A wait that runs out sets the program's error
+ * word and its kernel returns; togb_program_result then reports
+ * TOGB_ERR_TIMEOUT (and clears the word, so the next run starts clean).
+ * cycles <= 0 restores the default, 2e9 (about one second at 2 GHz).  The
+ * reference has no device waits; its only timeout is the host-side SIGALRM of
+ * util.TimeoutTimer (src/util/util.py:13-122). */
+togb_status togb_program_set_wait_limit(togb_program* prog, int64_t cycles);
+
 /* Per-join device time of the last run with togb_program_set_timing(prog, 1):
  * `ms[j]` for each join in post-order (n = num_joins). */
 togb_status togb_program_set_timing(togb_program* prog, int enable);
@@ -206,9 +217,10 @@ togb_status togb_probe_peak(int kind, void* stream, double* flops_per_second);
  * live in one file-scope device array of TOGB_STATIC_SCRATCH_BYTES (32 MiB),
  * held by every GPU that loads the library until exit; a program that needs
  * more than that for a single slice is rejected with TOGB_ERR_OOM and a message
- * giving both sizes.  The first call on a device looks up the array's address
- * (make it before any stream capture).  All calls share the array: calls whose
- * work overlaps on the GPU race, so serialise them.  Queued on `stream`. */
+ * giving both sizes.  The first call in each CUDA context (per device, and
+ * again after a cudaDeviceReset) looks up the array's address: make it before
+ * any stream capture.  All calls share the array: calls whose work overlaps on
+ * the GPU race, so serialise them.  Queued on `stream`. */
 togb_status togb_contract_static_f64(const togb_program_desc* desc, const double* d_leaf_values,
                                      double* d_out, void* stream);
 

@@ -3,7 +3,8 @@
 Test infrastructure only. Nothing in the product imports this file.
 
 What it builds, from the sources where they lie in the reference checkout
-(default ``/root/reference``; override with ``TOGB_REFERENCE_ROOT``):
+(``TOGB_REFERENCE_ROOT``, by default a ``reference`` directory beside the
+repository):
 
 * the five Cython (C++ mode) modules listed by ``src/setup.py:4``
   (``*/*.pyx``), cythonized into ``oracle/_ref/cy`` and compiled into
@@ -28,7 +29,10 @@ OUT = os.path.join(HERE, "_ref")
 
 
 def reference_root():
-    return os.environ.get("TOGB_REFERENCE_ROOT", "/root/reference")
+    """The reference checkout: ``TOGB_REFERENCE_ROOT``, else ``../reference``
+    next to this repository."""
+    default = os.path.join(os.path.dirname(HERE), os.pardir, "reference")
+    return os.path.normpath(os.environ.get("TOGB_REFERENCE_ROOT", default))
 
 
 def flowcutter_path():

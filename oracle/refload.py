@@ -32,7 +32,10 @@ _EXTENSIONS = (
 
 
 def reference_src():
-    return os.path.join(os.environ.get("TOGB_REFERENCE_ROOT", "/root/reference"), "src")
+    """``src/`` of the reference checkout: ``TOGB_REFERENCE_ROOT``, else
+    ``../reference`` next to this repository."""
+    default = os.path.join(os.path.dirname(HERE), os.pardir, "reference")
+    return os.path.join(os.path.normpath(os.environ.get("TOGB_REFERENCE_ROOT", default)), "src")
 
 
 def available():

@@ -12,14 +12,19 @@ and ``execution.py`` use it): ``add_argument``, ``get_entry_size``,
 
 ``contract_sliced`` is the hot path.  It flattens the plan
 (:func:`tensororder_gb300.program.from_plan`), hands it to libtogb and runs the
-slices in chunks: each C call returns after queueing a bounded number of
-slices, so the reference's SIGALRM timeouts (``util.py:13-122``) still fire
-between chunks.  A device allocation failure raises the reference's
+slices as a sequence of calls of bounded device time (about
+``max_call_seconds`` each, sized from the measured time of the previous call).
+After queueing a call it waits by polling a CUDA event from Python, so the
+reference's SIGALRM timeout (``util.py:32-39`` raises ``TimeoutError`` from
+the signal handler) fires mid-count, with at most one call's work left on the
+device.  A device allocation failure raises the reference's
 ``OutOfMemoryError`` (``base_api.py:4``), whose handler in ``execution.py:134-142``
 re-slices the plan and retries.  Nothing here falls back to a CPU path: if the
 CUDA library or device is missing the call fails.
 """
 from __future__ import annotations
+
+import time
 
 import numpy as np
 
@@ -39,6 +44,9 @@ class GB300API:
     """Execution backend; ``mode`` is ``runtime.MODE_F64`` or ``runtime.MODE_SPLIT``."""
 
     slices_per_call = 1 << 14  # upper bound on slices queued by one C call
+    max_call_seconds = 0.25    # target device time of one call (timeout granularity)
+    # device rate for sizing the first call before any has been timed (FLOP/s)
+    _first_call_rate = {runtime.MODE_F64: 1.0e12, runtime.MODE_SPLIT: 5.0e13}
 
     def __init__(self, mode=runtime.MODE_F64, device=0):
         self._mode = mode
@@ -119,20 +127,44 @@ class GB300API:
         value = self._run(prog, num_slice_limit)
         return value[()] if np.ndim(value) == 0 else value
 
-    def _run(self, prog, num_slice_limit):
+    def _stream(self):
         import torch
 
+        return torch.cuda.current_stream(self._device)
+
+    @staticmethod
+    def _wait(stream):
+        """Wait for the work queued on ``stream`` while returning to the
+        interpreter between polls, so a pending signal handler (the
+        reference's SIGALRM timeout) runs and may raise."""
+        import torch
+
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        t0 = time.perf_counter()
+        while not ev.query():
+            if time.perf_counter() - t0 > 2e-3:
+                time.sleep(2e-4)
+
+    def _run(self, prog, num_slice_limit):
         n = prog.num_slices if num_slice_limit is None else min(prog.num_slices, int(num_slice_limit))
         try:
             dp = runtime.DeviceProgram(prog, self._device)
             self.last_program = dp
-            stream = torch.cuda.current_stream(self._device)
+            stream = self._stream()
             dp.reset(stream)
             ws = dp.allocate_workspace(self._mode, max(n, 1))
+            # First call sized from the FLOP count, later ones from the measured
+            # time per slice of the previous call.
+            per_slice = max(float(dp.info.flops_per_slice), 1.0) / self._first_call_rate[self._mode]
             s = 0
             while s < n:
-                e = min(n, s + self.slices_per_call)
+                k = int(min(self.slices_per_call, max(1, self.max_call_seconds / max(per_slice, 1e-9))))
+                e = min(n, s + k)
+                t0 = time.perf_counter()
                 dp.run(self._mode, s, e, workspace=ws, stream=stream)
+                self._wait(stream)
+                per_slice = (time.perf_counter() - t0) / (e - s)
                 s = e
             return dp.result(stream)
         except runtime.DeviceOutOfMemory as exc:

@@ -67,6 +67,7 @@ struct JoinDesc {
   int32_t c_natural;   // output stored C[m][n] row-major, slices contiguous: address = linear index
   Runs r_inv_m, r_inv_n;  // output address bits -> m / n bits (inverse deposit of c_s_m / c_s_n)
   int32_t* err;        // device error word: set to 1 when a bounded wait gives up (may be null)
+  int64_t wait_cycles; // SM clock cycles a pipeline wait may last before the kernel gives up
 };
 
 // Root reduction: adds every slice's root tensor into the compensated FP64
@@ -78,6 +79,9 @@ struct RootDesc {
 };
 
 namespace togb {
+
+// Default limit of a device-side wait: about one second at 2 GHz.
+constexpr int64_t kDefaultWaitCycles = 2000000000ll;
 
 enum Kernel { K_DIRECT = 0, K_TILED = 1, K_REDUCE = 2, K_UMMA = 3 };
 
@@ -122,9 +126,13 @@ struct OnceList {
   int32_t total_tiles;
   uint32_t* counters;        // device [1 + n]: next tile, then published tiles per join (zero before the launch)
   int32_t* err;              // set when a wait expires
+  int64_t wait_cycles;       // SM clock cycles a producer wait may last before the CTA gives up
 };
 cudaError_t launch_once_list(int mode, const OnceList& ol, cudaStream_t st);
 
+// Streaming multiprocessors of the current device (cached per device).
+constexpr int kMaxDevices = 256;
+int sm_count();
 // Which thread-per-output variant a K_DIRECT join runs: 0 k_direct,
 // 1 k_direct_staged, 2 k_stream (m-fast A), 3 k_stream (k-fast A).
 int direct_variant(int mode, const JoinDesc& jd);

@@ -28,6 +28,7 @@
 //    on the IEEE bits, valid because every entry is >= 0).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstring>
 #include <type_traits>
 
@@ -594,8 +595,6 @@ __global__ void __launch_bounds__(kThreads, (KK * NN <= 4 || (KK * NN == 8 && KK
 // K <= 16, the compensated 16-term chunks above), so the results equal the
 // unfused launches bit for bit.
 
-constexpr long long kOnceWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
-
 __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
   uint32_t v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -730,7 +729,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_once_list(const __grid_constant
           const uint32_t ga = da >= 0 ? ld_acquire_u32(ol.counters + 1 + da) : 0u;
           const uint32_t gb = db >= 0 ? ld_acquire_u32(ol.counters + 1 + db) : 0u;
           if (ga >= na && gb >= nb) break;
-          if (*err || clock64() - t0 > kOnceWaitCycles) {
+          if (*err || clock64() - t0 > ol.wait_cycles) {
             bad = 1;
             break;
           }
@@ -1215,6 +1214,59 @@ __global__ void k_root(const __grid_constant__ RootDesc rd, const int64_t* __res
   }
 }
 
+// Exact sum of two doubles as a rounded sum plus its rounding error (Neumaier's
+// branch of Knuth's two-sum).
+__device__ __forceinline__ double two_sum_err(double a, double b, double t) {
+  return fabs(a) >= fabs(b) ? (a - t) + b : (b - t) + a;
+}
+
+// The root reduction for roots of few entries (a count has one): one CTA per
+// root entry.  Thread i takes slices i, i + 256, ... in slice order into a
+// compensated sum; the 256 (sum, compensation) pairs are then combined by a
+// fixed pairwise tree of two-sums and the chunk's total is added into the
+// accumulator.  The combination order depends only on the slice count, so
+// every run gives the same bits; the error stays a few units in the last
+// place of the total (compensated at every level).
+template <int MODE, class T>
+__global__ void __launch_bounds__(kThreads) k_root_tree(const __grid_constant__ RootDesc rd,
+                                                        const int64_t* __restrict__ d_s0, int nslices) {
+  __shared__ double ss[kThreads], sc[kThreads];
+  const int64_t e = blockIdx.x;
+  const int64_t s0 = d_s0 ? *d_s0 : 0;
+  const T* __restrict__ R = (const T*)rd.r.ptr;
+  const int64_t oe = dep(rd.r.r_outer, (uint64_t)e);
+  double sum = 0.0, comp = 0.0;
+  for (int b = threadIdx.x; b < nslices; b += kThreads) {
+    const int64_t o = slice_offset(rd.r, b, s0 + b) + oe;
+    double x = (double)R[o];
+    if (MODE == 1) {
+      if (rd.r.ptr_lo) x += (double)((const float*)rd.r.ptr_lo)[o];
+      x = ldexp(x, op_exp(rd.r, b));
+    }
+    const double t = sum + x;
+    comp += two_sum_err(sum, x, t);
+    sum = t;
+  }
+  ss[threadIdx.x] = sum;
+  sc[threadIdx.x] = comp;
+  __syncthreads();
+  for (int w = kThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      const double a = ss[threadIdx.x], b = ss[threadIdx.x + w];
+      const double t = a + b;
+      sc[threadIdx.x] += sc[threadIdx.x + w] + two_sum_err(a, b, t);
+      ss[threadIdx.x] = t;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double a = rd.acc_sum[e], b = ss[0];
+    const double t = a + b;
+    rd.acc_comp[e] += sc[0] + two_sum_err(a, b, t);
+    rd.acc_sum[e] = t;
+  }
+}
+
 __global__ void k_set_s0(int64_t* p, int64_t v) { *p = v; }
 
 // One CTA per leaf: the values of OrTensor / VariableTensor leaves from their
@@ -1314,13 +1366,7 @@ int grid_for(int64_t work) {
 template <class Kern>
 void staged_launch(Kern kern, const JoinDesc& jd, const StageInfo& si, const int64_t* s0, int nslices,
                    int64_t tiles, size_t bytes, cudaStream_t st) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
+  const int sms = sm_count();
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, bytes) != cudaSuccess || per_sm < 1)
@@ -1455,6 +1501,25 @@ bool launch_stream(int mode, const JoinDesc& jd, const int64_t* s0, int nslices,
 
 }  // namespace
 
+int sm_count() {
+  // Per device, filled on first use; concurrent first calls store the same value.
+  static std::atomic<int> sms[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return 1;
+  }
+  int n = sms[dev].load(std::memory_order_relaxed);
+  if (n <= 0) {
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+      cudaGetLastError();
+      return 1;
+    }
+    sms[dev].store(n, std::memory_order_relaxed);
+  }
+  return n;
+}
+
 int direct_variant(int mode, const JoinDesc& jd) {
   bool kfast = false;
   if (stream_ok(mode, jd, kfast)) return kfast ? 3 : 2;
@@ -1521,13 +1586,7 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
 
 cudaError_t launch_once_list(int mode, const OnceList& ol, cudaStream_t st) {
   if (ol.n <= 0 || ol.total_tiles <= 0) return cudaSuccess;
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
+  const int sms = sm_count();
   int per_sm = 0;
   cudaError_t e = mode == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<0, double>, kThreads, 0)
                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<1, float>, kThreads, 0);
@@ -1540,7 +1599,13 @@ cudaError_t launch_once_list(int mode, const OnceList& ol, cudaStream_t st) {
 }
 
 cudaError_t launch_root(int mode, const RootDesc& rd, const int64_t* s0, int nslices, cudaStream_t st) {
-  const int g = grid_for(1ll << rd.r.outer_bits);
+  const int64_t E = 1ll << rd.r.outer_bits;
+  if (E <= 1024) {  // few root entries: a CTA per entry, slices across its threads
+    if (mode == 0) k_root_tree<0, double><<<(unsigned)E, kThreads, 0, st>>>(rd, s0, nslices);
+    else k_root_tree<1, float><<<(unsigned)E, kThreads, 0, st>>>(rd, s0, nslices);
+    return cudaGetLastError();
+  }
+  const int g = grid_for(E);
   if (mode == 0) k_root<0, double><<<g, kThreads, 0, st>>>(rd, s0, nslices);
   else k_root<1, float><<<g, kThreads, 0, st>>>(rd, s0, nslices);
   return cudaGetLastError();

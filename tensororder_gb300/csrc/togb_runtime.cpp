@@ -159,6 +159,7 @@ struct togb_program {
   double* d_acc = nullptr;  // [2 * 2^root_rank]: sum then compensation
   int64_t* d_s0 = nullptr;
   int32_t* d_err = nullptr; // set by a kernel whose bounded wait expired
+  int64_t wait_cycles = togb::kDefaultWaitCycles;  // limit of every device-side pipeline wait
   void* own_ws = nullptr;
   size_t own_ws_bytes = 0;
   cudaStream_t cap_stream = nullptr;
@@ -614,6 +615,7 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
     togb::make_inverse_runs(jd.c_s_n, jd.nb, &jd.r_inv_n);
     jd.c_natural = is_natural(jd);
     jd.err = p->d_err;
+    jd.wait_cycles = p->wait_cycles;
     if (mode == TOGB_MODE_SPLIT) {
       jd.c_exp = J.dep ? w.per_exp + (int64_t)J.slot * B : w.once_exp + J.slot;
       jd.c_max = J.dep ? w.per_max + (int64_t)J.slot * B : w.once_max + J.slot;
@@ -811,6 +813,7 @@ togb_status prepare_once_fused(togb_program* p, int mode) {
     S.ol.tile_join = (const int32_t*)(d + off_tj[g]);
     S.ol.counters = p->d_once_ctr + off_ctr[g];
     S.ol.err = p->d_err;
+    S.ol.wait_cycles = p->wait_cycles;
   }
   p->once_segs_mode = mode;
   return TOGB_OK;
@@ -1300,6 +1303,18 @@ togb_status togb_program_kernel_allowed(const togb_program* p, int mode, int32_t
   return TOGB_OK;
 }
 
+togb_status togb_program_set_wait_limit(togb_program* p, int64_t cycles) {
+  if (!p) return fail(TOGB_ERR_INVALID, "null program");
+  const int64_t c = cycles > 0 ? cycles : togb::kDefaultWaitCycles;
+  if (c != p->wait_cycles) {
+    p->wait_cycles = c;
+    clear_graphs(p);      // captured launches carry the old limit
+    p->cur_mode = -1;     // descriptors are rebuilt on the next run
+    p->once_segs_mode = -1;
+  }
+  return TOGB_OK;
+}
+
 togb_status togb_program_set_timing(togb_program* p, int enable) {
   if (!p) return fail(TOGB_ERR_INVALID, "null program");
   p->timing = enable != 0;
@@ -1344,8 +1359,11 @@ togb_status togb_program_run(togb_program* p, int mode, int64_t begin, int64_t e
   }
   char* ws = (char*)(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
   const int64_t usable = (int64_t)ws_bytes - (int64_t)(ws - (char*)workspace) - ws_once(p, mode);
+  // Slices per chunk: what the workspace holds, independent of this call's
+  // range, so a count queued as several calls over consecutive ranges keeps
+  // one set of descriptors and graphs.
   int64_t B = usable > 0 ? usable / per : 0;
-  B = std::min<int64_t>(B, std::min<int64_t>(want, 65535));
+  B = std::min<int64_t>(B, std::min<int64_t>(p->num_slices, 65535));
   if (B < 1) return fail(TOGB_ERR_OOM, "workspace smaller than one slice");
   if (mode != p->cur_mode || B != p->cur_B || ws != p->cur_ws) {
     clear_graphs(p);
@@ -1379,7 +1397,9 @@ togb_status togb_program_result(togb_program* p, void* stream, double* out, doub
   TOGB_CUDA(cudaMemcpy(&err, p->d_err, 4, cudaMemcpyDeviceToHost));
   if (err) {
     TOGB_CUDA(cudaMemset(p->d_err, 0, 4));
-    return fail(TOGB_ERR_TIMEOUT, "a tensor-core kernel gave up waiting for its MMAs; the result is invalid");
+    return fail(TOGB_ERR_TIMEOUT,
+                "a device-side wait ran out of its limit (a fused slice-invariant list waiting for a producer "
+                "tile, or a tensor-core join waiting in its load/MMA/read-out pipeline); the result is invalid");
   }
   std::vector<double> h(2 * E);
   TOGB_CUDA(cudaMemcpy(h.data(), p->d_acc, 2 * E * 8, cudaMemcpyDeviceToHost));
@@ -1621,6 +1641,7 @@ togb_status togb_tensordot_f64(const double* a, int32_t ra, const double* b, int
   togb::make_inverse_runs(jd.c_s_m, jd.mb, &jd.r_inv_m);
   togb::make_inverse_runs(jd.c_s_n, jd.nb, &jd.r_inv_n);
   jd.c_natural = is_natural(jd);
+  jd.wait_cycles = togb::kDefaultWaitCycles;
   const int kernel = choose_kernel(jd.mb, jd.nb, jd.kb);
   cudaError_t e = togb::launch_join(TOGB_MODE_F64, kernel, jd, nullptr, 1, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "tensordot launch");

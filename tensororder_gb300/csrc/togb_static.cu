@@ -11,15 +11,19 @@
 //
 // The scratch is the file-scope array below: TOGB_STATIC_SCRATCH_BYTES of
 // device memory that every GPU which loads this library holds until the
-// process exits.  The first call on a device looks up the array's device
-// address with cudaGetSymbolAddress while that device is current (in host
-// code the symbol is only a host-side stand-in: handing it to a kernel would
-// fault, or on systems where the GPU can reach host memory read the wrong
-// memory).  Make that first call on each device before any stream capture
-// begins.  Every call shares the one array and leaves its contents behind;
+// process exits.  The first call in a CUDA context looks up the array's
+// device address with cudaGetSymbolAddress while that device is current (in
+// host code the symbol is only a host-side stand-in: handing it to a kernel
+// would fault, or on systems where the GPU can reach host memory read the
+// wrong memory).  The address is cached per device together with the unique id
+// of the context it was looked up in; after a cudaDeviceReset the primary
+// context is new, the module is loaded again and the array may move, so the
+// next call looks it up again.  Make the first call in each context before any
+// stream capture begins.  Every call shares the one array and leaves its contents behind;
 // the accumulator is cleared at the start of each call, and calls whose work
 // overlaps on the GPU race on the array, so serialise them (one stream, or
 // events between streams).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -32,9 +36,27 @@ static __device__ __align__(256) unsigned char g_togb_static_scratch[TOGB_STATIC
 
 namespace {
 
-constexpr int kMaxDevices = 256;
+using togb::kMaxDevices;
 std::mutex g_setup_mutex;
 void* g_scratch_address[kMaxDevices] = {};
+unsigned long long g_scratch_context[kMaxDevices] = {};  // cuCtxGetId of the context the address belongs to
+
+// The two driver calls, resolved through the runtime so the library carries no
+// link-time dependency on the driver library.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+template <class Fn>
+Fn driver_fn(const char* name) {
+  void* f = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (Fn)f;
+}
 
 }  // namespace
 
@@ -45,10 +67,23 @@ extern "C" togb_status togb_contract_static_f64(const togb_program_desc* desc, c
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return togb::report(TOGB_ERR_CUDA, cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return togb::report(TOGB_ERR_UNSUPPORTED, "device index out of range");
+  // The id of the current context tells whether a cached address is still
+  // valid.  With no context current yet (this is the process's first CUDA
+  // call), cudaSetDevice creates and binds the device's primary context; a
+  // context the caller made current is left as it is.
+  static const CtxGetCurrentFn get_current = driver_fn<CtxGetCurrentFn>("cuCtxGetCurrent");
+  static const CtxGetIdFn get_id = driver_fn<CtxGetIdFn>("cuCtxGetId");
+  if (!get_current || !get_id) return togb::report(TOGB_ERR_CUDA, "driver context queries unavailable");
+  CUcontext ctx = nullptr;
+  unsigned long long ctx_id = 0;
+  if (get_current(&ctx) == CUDA_SUCCESS && !ctx && (e = cudaSetDevice(dev)) != cudaSuccess)
+    return togb::report(TOGB_ERR_CUDA, cudaGetErrorString(e));
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &ctx_id) != CUDA_SUCCESS)
+    return togb::report(TOGB_ERR_CUDA, "no current CUDA context for the static scratch");
   void* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_address[dev]) {
+    if (!g_scratch_address[dev] || g_scratch_context[dev] != ctx_id) {
       void* addr = nullptr;
       e = cudaGetSymbolAddress(&addr, g_togb_static_scratch);
       if (e != cudaSuccess || !addr) {
@@ -57,6 +92,7 @@ extern "C" togb_status togb_contract_static_f64(const togb_program_desc* desc, c
                                             cudaGetErrorString(e)).c_str());
       }
       g_scratch_address[dev] = addr;
+      g_scratch_context[dev] = ctx_id;
     }
     scratch = g_scratch_address[dev];
   }

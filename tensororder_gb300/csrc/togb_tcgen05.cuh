@@ -10,7 +10,7 @@ namespace {
 constexpr int kBM = 128;          // UMMA M
 constexpr int kBK = 32;           // K per chunk (4 MMAs of K = 8)
 constexpr int kUmmaThreads = 256;  // 8 warps: warps w and w+4 share TMEM lanes 32*(w%4)
-constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
+constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz: drains on the abort path
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -32,12 +32,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait for phase `parity` of the mbarrier at `addr`.
-__device__ bool mbar_wait_bounded(uint32_t addr, uint32_t parity) {
+// Bounded wait for phase `parity` of the mbarrier at `addr`: at most `limit`
+// SM clock cycles (the fixed drain limit by default).
+__device__ bool mbar_wait_bounded(uint32_t addr, uint32_t parity, long long limit = kWaitCycles) {
   if (mbar_try_wait(addr, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_wait(addr, parity))
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 
@@ -143,15 +144,16 @@ __device__ __forceinline__ void mbar_arrive(uint32_t addr) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(addr) : "memory");
 }
 
-// Bounded wait that also gives up as soon as another role of the CTA raised
-// `*abort` (a shared flag): every role of a warp-specialised kernel leaves
-// within about a second of the first expired wait.
-__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t addr, uint32_t parity, volatile int* abort) {
+// Bounded wait (at most `limit` SM clock cycles) that also gives up as soon
+// as another role of the CTA raised `*abort` (a shared flag): every role of a
+// warp-specialised kernel leaves within one limit of the first expired wait.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t addr, uint32_t parity, volatile int* abort,
+                                                   long long limit) {
   if (mbar_try_wait(addr, parity)) return true;  // the common case: no clock read
   const long long t0 = clock64();
   while (!mbar_try_wait(addr, parity)) {
     if (*abort) return false;
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   }
   return true;
 }

@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) k_umma(const __grid_constant_
       // completed before the read-out of chunk c-2 in the previous iteration.
       if constexpr (TMA) {
         if (tid == 0 && c + L::NRAW - 1 < nchunks) issue_tma(c + L::NRAW - 1);
-        if (!mbar_wait_bounded(smem_u32(&mbar_full[c % L::NRAW]), (c / L::NRAW) & 1)) timeout_sh = 1;
+        if (!mbar_wait_bounded(smem_u32(&mbar_full[c % L::NRAW]), (c / L::NRAW) & 1, jd.wait_cycles)) timeout_sh = 1;
         __syncthreads();
         if (timeout_sh) { ok = false; break; }
       } else {
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) k_umma(const __grid_constant_
     if (c >= 1) {
       // Read out chunk c-1 once its MMAs completed.
       const int pc = c - 1, pst = pc & 1;
-      if (tid == 0 && !mbar_wait_bounded(smem_u32(&mbar[pst]), (pc >> 1) & 1)) timeout_sh = 1;
+      if (tid == 0 && !mbar_wait_bounded(smem_u32(&mbar[pst]), (pc >> 1) & 1, jd.wait_cycles)) timeout_sh = 1;
       __syncthreads();
       if (timeout_sh) { ok = false; break; }
       tc_fence_after();

@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
         const int asl = jd.a.batch_stride ? b : 0, bsl = jd.b.batch_stride ? b : 0;
         for (int c = 0; c < nchunks; ++c, ++gc) {
           const int st = gc % NR, u = gc / NR;
-          if (gc >= NR && !mbar_wait_or_abort(smem_u32(&rawfree[st]), (u - 1) & 1, abort)) {
+          if (gc >= NR && !mbar_wait_or_abort(smem_u32(&rawfree[st]), (u - 1) & 1, abort, jd.wait_cycles)) {
             *abort = 1;
             break;
           }
@@ -187,13 +187,13 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
       for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
         for (int c = 0; c < nchunks && ok; ++c, ++gc) {
           const int st = gc % NC, u = gc / NC;
-          if (!mbar_wait_or_abort(smem_u32(&conv[st]), u & 1, abort)) { ok = false; break; }
+          if (!mbar_wait_or_abort(smem_u32(&conv[st]), u & 1, abort, jd.wait_cycles)) { ok = false; break; }
           tc_fence_after();
           const uint32_t a_hi = sbase + NR * L::RAW + st * L::CONV, b_hi = a_hi + L::A_BYTES;
           const uint32_t a_lo = a_hi + L::RAW, b_lo = a_lo + L::A_BYTES;
           {
             const int set = gw % NSETS;
-            if (gw >= NSETS && !mbar_wait_or_abort(smem_u32(&acce[set]), (gw / NSETS - 1) & 1, abort)) {
+            if (gw >= NSETS && !mbar_wait_or_abort(smem_u32(&acce[set]), (gw / NSETS - 1) & 1, abort, jd.wait_cycles)) {
               ok = false;
               break;
             }
@@ -243,8 +243,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
       const float fa = pow2f(op_shift(jd.a, b)), fb = pow2f(op_shift(jd.b, b));
       for (int c = 0; c < nchunks; ++c, ++gc) {
         const int rs = gc % NR, ru = gc / NR, cs = gc % NC, cu = gc / NC;
-        const bool got = mbar_wait_or_abort(smem_u32(&full[rs]), ru & 1, abort) &&
-                         (gc < NC || mbar_wait_or_abort(smem_u32(&cfree[cs]), (cu - 1) & 1, abort));
+        const bool got = mbar_wait_or_abort(smem_u32(&full[rs]), ru & 1, abort, jd.wait_cycles) &&
+                         (gc < NC || mbar_wait_or_abort(smem_u32(&cfree[cs]), (cu - 1) & 1, abort, jd.wait_cycles));
         if (!__all_sync(0xffffffffu, got)) {  // warp-uniform exit
           *abort = 1;
           ok = false;
@@ -299,8 +299,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
         for (int w = 0; w < nwin;) {
           const bool two = w + 1 < nwin;
           const int set0 = gw % NSETS, set1 = (gw + 1) % NSETS;
-          const bool got = mbar_wait_or_abort(smem_u32(&accf[set0]), (gw / NSETS) & 1, abort) &&
-                           (!two || mbar_wait_or_abort(smem_u32(&accf[set1]), ((gw + 1) / NSETS) & 1, abort));
+          const bool got = mbar_wait_or_abort(smem_u32(&accf[set0]), (gw / NSETS) & 1, abort, jd.wait_cycles) &&
+                           (!two || mbar_wait_or_abort(smem_u32(&accf[set1]), ((gw + 1) / NSETS) & 1, abort, jd.wait_cycles));
           if (!__all_sync(0xffffffffu, got)) {
             *abort = 1;
             break;
@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
       } else {
         for (int w = 0; w < nwin; ++w, ++gw) {
           const int set = gw % NSETS;
-          if (!__all_sync(0xffffffffu, mbar_wait_or_abort(smem_u32(&accf[set]), (gw / NSETS) & 1, abort))) {
+          if (!__all_sync(0xffffffffu, mbar_wait_or_abort(smem_u32(&accf[set]), (gw / NSETS) & 1, abort, jd.wait_cycles))) {
             *abort = 1;
             break;
           }
@@ -396,19 +396,6 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
   __syncthreads();
   if (warp == 1) tmem_dealloc(tmem, kCols);
   if (tid == 0 && abort_sh && jd.err) atomicExch(jd.err, 1);
-}
-
-int sm_count() {
-  static int sms[64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64) dev = 0;
-  if (!sms[dev]) {
-    int n = 0;
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    sms[dev] = n > 0 ? n : 1;
-  }
-  return sms[dev];
 }
 
 template <int BN, int NR, int NC, bool PAIRS>

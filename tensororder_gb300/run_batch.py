@@ -34,6 +34,35 @@ def load(path, limit=None):
     return progs, refs, items
 
 
+def reference_errors(progs, items, counts, mode=runtime.MODE_SPLIT, device=0, stream=None, max_prefix_flops=None):
+    """Relative errors of a batch against the reference's counts recorded in
+    the batch file: ``counts[i]`` (the batch's full count) for instances with
+    the reference's full count, and for the others a separate contraction of
+    the recorded slice prefix (``reference_prefix``: the first P slices in
+    ``itertools.product`` order, the reference's ``num_slice_limit``,
+    ``base_api.py:23-24``).  Instances whose prefix work exceeds
+    ``max_prefix_flops`` are skipped.  Returns ``(full, prefix)`` arrays of
+    relative errors."""
+    full, prefix = [], []
+    for i, it in enumerate(items):
+        if it["reference_float64"] is not None:
+            full.append(abs(counts[i] - it["reference_float64"]) / abs(it["reference_float64"]))
+            continue
+        pre = it.get("reference_prefix")
+        if not pre:
+            continue
+        P = int(pre["slices"])
+        if max_prefix_flops is not None and it["executed_flops"] * P / (1 << it["slice_groups"]) > max_prefix_flops:
+            continue
+        dp = runtime.DeviceProgram(progs[i], device)
+        dp.reset(stream)
+        dp.run(mode, 0, P, workspace=dp.allocate_workspace(mode, P), stream=stream)
+        got = float(dp.result(stream).reshape(-1)[0])
+        dp.close()
+        prefix.append(abs(got - pre["float64"]) / abs(pre["float64"]))
+    return np.array(full), np.array(prefix)
+
+
 def time_steps(ex, steps, warmup, stream):
     import torch
 
@@ -75,10 +104,12 @@ def main(argv=None):
     work = ex.work()
     ex.close()
     have = ~np.isnan(refs)
-    rel = np.abs(counts[have] - refs[have]) / np.abs(refs[have])
+    full, prefix = reference_errors(progs, items, counts, mode, stream=stream)
+    rel = np.concatenate([full, prefix])
     out.update({"ms_per_step": ms, "counts_per_s": len(progs) * 1e3 / ms,
                 "executed_tflops": work["executed_flops"] / (ms * 1e-3) / 1e12,
-                "slices": work["slices"], "checked_against_reference": int(have.sum()),
+                "slices": work["slices"], "checked_against_reference": int(rel.size),
+                "checked_full_count": int(full.size), "checked_slice_prefix": int(prefix.size),
                 "max_rel_err": float(rel.max()) if rel.size else None})
     if args.tune:
         tuner = batch.Autotuner(mode)

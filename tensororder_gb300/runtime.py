@@ -93,7 +93,7 @@ EXPORTS = [
     "togb_mlp_param_count", "togb_mlp_scratch_floats", "togb_mlp_forward", "togb_mlp_loss_grad", "togb_mlp_adam",
     "togb_batch_create", "togb_batch_run", "togb_batch_results", "togb_batch_destroy",
     "togb_program_create_host", "togb_program_describe", "togb_program_create_compact",
-    "togb_program_launch_count",
+    "togb_program_launch_count", "togb_program_set_wait_limit",
 ]
 
 KERNEL_NAMES = {0: "direct", 1: "tiled", 2: "reduce", 3: "tensor"}
@@ -133,6 +133,7 @@ def lib():
     L.togb_program_joins.argtypes = [c_void, ctypes.c_int, _i32p, ctypes.c_int32]
     L.togb_program_launch_count.argtypes = [c_void, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
     L.togb_program_set_kernel.argtypes = [c_void, ctypes.c_int, ctypes.c_int32, ctypes.c_int32]
+    L.togb_program_set_wait_limit.argtypes = [c_void, ctypes.c_int64]
     L.togb_program_kernel_allowed.argtypes = [c_void, ctypes.c_int, ctypes.c_int32, ctypes.c_int32, _i32p]
     L.togb_batch_create.argtypes = [ctypes.POINTER(c_void), ctypes.c_int32, ctypes.c_int, ctypes.POINTER(c_void),
                                     ctypes.POINTER(ctypes.c_size_t), ctypes.c_int32, ctypes.POINTER(c_void)]
@@ -342,6 +343,12 @@ class DeviceProgram:
     def set_timing(self, enable=True):
         check(lib().togb_program_set_timing(self._h, 1 if enable else 0))
 
+    def set_wait_limit(self, cycles=0):
+        """Limit of every device-side wait in SM clock cycles (<= 0: the
+        default, about one second).  An expired wait makes :meth:`result`
+        raise ``TogbError`` with status ``ERR_TIMEOUT``."""
+        check(lib().togb_program_set_wait_limit(self._h, int(cycles)))
+
     def join_times(self):
         n = int(self.info.num_joins)
         out = (ctypes.c_float * n)()
@@ -430,7 +437,52 @@ def contract_static_f64(program: Program, leaf_values, out, stream=None):
     the concatenated leaf parents (``DeviceProgram``'s layout) and ``out`` a
     float64 CUDA tensor of ``2**root_rank`` entries; both belong to the caller.
     Calls that overlap on the GPU share one scratch array and must not run
-    concurrently."""
+    concurrently.
+
+    Both tensors are checked before anything is queued (``ValueError``): the
+    library receives raw addresses and sizes them from the program alone, so a
+    short, strided, mistyped or foreign-device buffer would be read or written
+    out of bounds on the device."""
+    import torch
+
+    n_values = sum(1 << l.rank for l in program.leaves)
+    n_out = 1 << program_root_rank(program)
+    for name, t, want in (("leaf_values", leaf_values, None), ("out", out, n_out)):
+        if not isinstance(t, torch.Tensor) or t.dtype != torch.float64:
+            raise ValueError("%s must be a float64 torch tensor" % name)
+        if not t.is_contiguous():
+            raise ValueError("%s must be contiguous" % name)
+        if want is not None and t.numel() != want:
+            raise ValueError("%s holds %d entries; the root tensor has %d" % (name, t.numel(), want))
+    if leaf_values.numel() < n_values:
+        raise ValueError("leaf_values holds %d entries; the program's leaves need %d"
+                         % (leaf_values.numel(), n_values))
+    if not (leaf_values.is_cuda and out.is_cuda):
+        raise ValueError("leaf_values and out must be CUDA tensors")
+    if leaf_values.device != out.device:
+        raise ValueError("leaf_values (%s) and out (%s) are on different devices" % (leaf_values.device, out.device))
+    with torch.cuda.device(out.device):
+        return _contract_static_f64(program, leaf_values, out, stream)
+
+
+def program_root_rank(program: Program):
+    """Rank of the final tensor over unsliced edges: the edges of the root
+    that the post-order walk leaves uncontracted (0 for a count)."""
+    from .program import join_edges
+
+    sliced = {e for g in program.slice_groups for e in g}
+    stack = []
+    for t in program.postorder:
+        if t >= 0:
+            stack.append([e for e in program.leaves[t].axes if e not in sliced])
+        else:
+            r = stack.pop()
+            l = stack.pop()
+            stack.append(join_edges(l, r)[2])
+    return len(stack[0])
+
+
+def _contract_static_f64(program, leaf_values, out, stream):
     leaves = program.leaves
     ranks = np.array([l.rank for l in leaves], dtype=np.int32)
     axes = np.array([a for l in leaves for a in l.axes] or [0], dtype=np.int32)

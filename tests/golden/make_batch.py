@@ -19,7 +19,7 @@ The reference's numpy FP64 count is recorded for instances whose executed work
 is below ``ref_flops`` (others carry ``null``; their parity is checked between
 the two GPU forms).
 
-Usage: ``python tensororder_gb300/plans/make_batch.py [count] [out]``.
+Usage: ``python tests/golden/make_batch.py [count] [out]``.
 """
 import contextlib
 import gzip
@@ -32,6 +32,7 @@ import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
+PLANS = os.path.join(ROOT, "tensororder_gb300", "plans")
 sys.path.insert(0, ROOT)
 
 from oracle import refload  # noqa: E402
@@ -39,7 +40,8 @@ from tensororder_gb300 import costmodel, instances  # noqa: E402
 from tensororder_gb300.program import from_plan  # noqa: E402
 
 
-def make_instance(i, base_seed=1000, v_max=52, timeout=1.0, ref_flops=2e9):
+def instance_plan(i, base_seed=1000, v_max=52, timeout=1.0):
+    """The reference plan of instance ``i``: ``(kind, size, planner, plan)``."""
     seed = base_seed + i
     rng = random.Random(seed)
     g = rng.randint(0, 8)
@@ -55,6 +57,13 @@ def make_instance(i, base_seed=1000, v_max=52, timeout=1.0, ref_flops=2e9):
     with contextlib.redirect_stdout(sink), contextlib.redirect_stderr(sink):
         plan = refload.plan_cnf(cnf, weights="cachet", planner=planner, seed=0, timeout=timeout,
                                 minimum_slice=g, rank_limit=30)
+    return kind, size, planner, plan
+
+
+def make_instance(i, base_seed=1000, v_max=52, timeout=1.0, ref_flops=2e9):
+    seed = base_seed + i
+    kind, size, planner, plan = instance_plan(i, base_seed, v_max, timeout)
+    sink = io.StringIO()
     prog = from_plan(plan)
     cost = costmodel.executed_cost(prog)
     ref = None
@@ -68,7 +77,7 @@ def make_instance(i, base_seed=1000, v_max=52, timeout=1.0, ref_flops=2e9):
 
 def main():
     count = int(sys.argv[1]) if len(sys.argv) > 1 else 512
-    out = sys.argv[2] if len(sys.argv) > 2 else os.path.join(HERE, "batch%d.json.gz" % count)
+    out = sys.argv[2] if len(sys.argv) > 2 else os.path.join(PLANS, "batch%d.json.gz" % count)
     t0 = time.time()
     items = []
     for i in range(count):

@@ -12,7 +12,7 @@ the reference nor a planner.
 * ``wvc300`` -- the same construction with n=300, sliced only as rank 30
   requires (the held-out instance of the learned cost model).
 
-Usage: ``python tensororder_gb300/plans/make_plans.py [name ...]``.
+Usage: ``python tests/golden/make_plans.py [name ...]``.
 """
 import gzip
 import json
@@ -22,6 +22,7 @@ import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
+PLANS = os.path.join(ROOT, "tensororder_gb300", "plans")
 sys.path.insert(0, ROOT)
 
 from oracle import refload  # noqa: E402
@@ -58,7 +59,7 @@ def make(name):
         "program": prog.to_dict(),
         "reference": {"float64": count, "seconds_here": elapsed, "cores_here": os.cpu_count()},
     }
-    with gzip.open(os.path.join(HERE, name + ".json.gz"), "wt") as f:
+    with gzip.open(os.path.join(PLANS, name + ".json.gz"), "wt") as f:
         json.dump(doc, f, separators=(",", ":"))
     print(name, prog.num_joins, "joins", prog.num_slices, "slices", count, "%.1fs" % elapsed)
 

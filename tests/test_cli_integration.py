@@ -41,3 +41,34 @@ def test_cli_selects_plugin(library, mode, monkeypatch, capsys):
     out = capsys.readouterr().out
     assert "Count: 2802717837" in out
     assert len(calls) == 1 and calls[0][1] == 4 and calls[0][2] == mode
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("library", ["gb300", "gb300-split"])
+def test_cli_counts_on_the_device(library, monkeypatch, capsys, cuda):
+    """The same CLI run with the real kernels: the count must come out of
+    libtogb.  Needs both the reference checkout and a GPU in one place."""
+    refload.load()
+    from tensororder_gb300 import api, launcher
+
+    runs = []
+    real = api.GB300API._run
+
+    def spy(self, prog, limit):
+        out = real(self, prog, limit)
+        runs.append(self.last_program is not None)
+        return out
+
+    monkeypatch.setattr(api.GB300API, "_run", spy)
+    monkeypatch.setattr(api, "_OOM", api._OOM)
+    cnf = os.path.join(refload.reference_src(), "..", "benchmarks", "cubic_vertex_cover", "cubic_vc_50_0.cnf")
+    monkeypatch.setattr(sys, "stdin", io.StringIO(open(cnf).read()))
+    monkeypatch.chdir(refload.REF_OUT)
+    with pytest.raises(SystemExit) as exc:
+        launcher.main(["--reference-src", refload.reference_src(), "tensororder", "--planner", "line-Flow",
+                       "--weights", "unweighted", "--tensor_library", library, "--timeout", "3",
+                       "--minimum_slice", "2"])
+    assert exc.value.code == 0
+    out = capsys.readouterr().out
+    assert ("Count: 2802717837" in out) if library == "gb300" else ("Count: 2802717" in out)
+    assert runs == [True]

@@ -61,3 +61,27 @@ def test_batch_rejects_duplicate_program(cuda):
     st = runtime.lib().togb_batch_create(h, 2, runtime.MODE_F64, p, b, 1, ctypes.byref(out))
     assert st == runtime.ERR_INVALID and not out.value
     dp.close()
+
+
+def test_batch512_every_instance_matches_reference(cuda):
+    """The 512-instance uneven batch (config 4) in the split form: the 291
+    instances with the reference's full count are checked on the batch's
+    counts, the other 221 on the reference's count of their first slices
+    (contracted separately), all within 1e-6.  The plain form is checked on
+    the prefixes of the cheaper instances within 1e-12."""
+    import os
+
+    from conftest import ROOT
+    from tensororder_gb300.run_batch import load, reference_errors
+
+    progs, refs, items = load(os.path.join(ROOT, "tensororder_gb300", "plans", "batch512.json.gz"))
+    ex = batch.BatchExecutor(progs, runtime.MODE_SPLIT, nstreams=16)
+    ex.run()
+    counts = ex.counts()
+    ex.close()
+    full, prefix = reference_errors(progs, items, counts, runtime.MODE_SPLIT)
+    assert full.size + prefix.size == 512
+    assert full.max() <= 1e-6 and prefix.max() <= 1e-6
+    _, prefix64 = reference_errors(progs, items, np.full(len(progs), np.nan), runtime.MODE_F64,
+                                   max_prefix_flops=2e10)
+    assert prefix64.size >= 100 and prefix64.max() <= 1e-12

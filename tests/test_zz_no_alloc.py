@@ -4,9 +4,11 @@ It exists for callers that cannot call cudaMalloc -- a process whose device
 memory is all owned by its own allocator, or a pipeline that cannot take the
 device-wide synchronisation of cudaMalloc/cudaFree.  These tests call it
 through the C ABI with caller-owned input and output buffers and check it
-against the allocating entry point (togb_program_*) within the plain-form
-tolerance, twice in a row, since every call reuses the same static scratch.
-This file sorts last so a failure here leaves the rest of the suite already run.
+against the allocating entry point (togb_program_*) and against the
+reference's own numpy FP64 count recorded in the golden fixture, within the
+plain-form tolerance, twice in a row, since every call reuses the same static
+scratch.  This file sorts last so a failure here leaves the rest of the suite
+already run.
 """
 import numpy as np
 import pytest
@@ -24,7 +26,9 @@ TOL = 1e-12
 def test_static_entry_matches_allocating_entry(name, cuda):
     import torch
 
-    prog = Program.from_dict(load_golden(name)["program"])
+    doc = load_golden(name)
+    prog = Program.from_dict(doc["program"])
+    reference = doc["reference"]["float64"]
     dp = runtime.DeviceProgram(prog)
     dp.reset()
     dp.run(runtime.MODE_F64)
@@ -37,17 +41,22 @@ def test_static_entry_matches_allocating_entry(name, cuda):
         runtime.contract_static_f64(prog, leaves, out)
         got = out.cpu().numpy()
         assert np.all(np.abs(got - want) <= TOL * np.abs(want))
+        assert abs(got[0] - reference) <= TOL * abs(reference)
 
 
 def test_static_entry_rejects_programs_beyond_its_scratch(cuda):
     import torch
 
-    # Two rank-14 tensors with no shared edge: the output has rank 28, i.e.
-    # 2 GiB per slice, far beyond the 32 MiB static scratch.
-    a = Leaf(list(range(14)), "dense", values=np.ones((2,) * 14))
-    b = Leaf(list(range(14, 28)), "dense", values=np.ones((2,) * 14))
-    prog = Program([a, b], [0, 1, -1])
-    leaves = torch.ones(2 << 14, dtype=torch.float64, device=cuda)
+    # Two rank-12 tensors with no shared edge: their outer product has rank
+    # 24, i.e. 128 MiB per slice, beyond the 32 MiB static scratch; two more
+    # leaves contract it back to a count.
+    ones = np.ones((2,) * 12)
+    a = Leaf(list(range(12)), "dense", values=ones)
+    b = Leaf(list(range(12, 24)), "dense", values=ones)
+    c = Leaf(list(range(12)), "dense", values=ones)
+    d = Leaf(list(range(12, 24)), "dense", values=ones)
+    prog = Program([a, b, c, d], [0, 1, -1, 2, -1, 3, -1])
+    leaves = torch.ones(4 << 12, dtype=torch.float64, device=cuda)
     out = torch.empty(1, dtype=torch.float64, device=cuda)
     with pytest.raises(runtime.DeviceOutOfMemory) as exc:
         runtime.contract_static_f64(prog, leaves, out)
