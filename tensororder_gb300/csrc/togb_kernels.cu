@@ -587,6 +587,106 @@ __global__ void __launch_bounds__(kThreads, (KK * NN <= 4 || (KK * NN == 8 && KK
   if (carry_b >= 0 && (threadIdx.x & (lanes - 1)) == 0) atomicMax(&jd.c_max[carry_b], v);
 }
 
+// Component j (a compile-time constant after unrolling) of a float4.
+__device__ __forceinline__ float f4_at(const float4& v, int j) {
+  return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+
+// k_stream's arithmetic with more loads in flight, for slices of at least
+// 32*U quads: each warp takes a block of 32*U consecutive quads of one slice
+// (lane l owns quads l, l + 32, ..., so every load and store instruction of
+// the warp covers consecutive 16-byte vectors), loads the slice's B and
+// normalisers once per block and issues all U*KK vector loads of A before any
+// arithmetic.  Per output the FMAs run in k_stream's order, so the results are
+// the same bits.
+template <int KK, int NN, bool KFAST, int LOGU>
+__global__ void __launch_bounds__(kThreads) k_stream_blk(const __grid_constant__ JoinDesc jd,
+                                                         const int64_t* __restrict__ d_s0, int nslices) {
+  constexpr int U = 1 << LOGU;
+  const int wb = jd.mb - 2 - 5 - LOGU;  // log2 of the warp blocks per slice
+  const int64_t blocks = (int64_t)nslices << wb;
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int mnb = jd.mb + jd.nb;
+  const int64_t s0 = d_s0 ? *d_s0 : 0;
+  const float* __restrict__ A = (const float*)jd.a.ptr;
+  const float* __restrict__ B = (const float*)jd.b.ptr;
+  const float* __restrict__ Blo = (const float*)jd.b.ptr_lo;
+  float* __restrict__ C = (float*)jd.c_ptr;
+  for (int64_t blk = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; blk < blocks; blk += nwarps) {
+    const int b = (int)(blk >> wb);
+    const int64_t s = s0 + b;
+    const uint64_t q0 = ((uint64_t)blk & ((1ull << wb) - 1)) << (5 + LOGU);  // first quad of the block
+    const int64_t abase = slice_offset(jd.a, b, s);
+    float4 x[U][KK];
+#pragma unroll
+    for (int i = 0; i < U; ++i) {
+      const uint64_t m0 = (q0 + (uint64_t)(lane + 32 * i)) << 2;
+      const int64_t ao = abase + dep(jd.a.r_outer, m0);
+#pragma unroll
+      for (int v = 0; v < KK; ++v)
+        x[i][v] = *reinterpret_cast<const float4*>(A + ao + (KFAST ? 4 * v : jd.a.ktab[v]));
+    }
+    const int sa = op_shift(jd.a, b), sb = op_shift(jd.b, b);
+    const float fa = pow2f(sa), fb = pow2f(sb);
+    const int64_t bbase = slice_offset(jd.b, b, s);
+    float bv[KK][NN], bl[KK][NN];
+#pragma unroll
+    for (int n = 0; n < NN; ++n) {
+      const int64_t o = bbase + dep(jd.b.r_outer, (uint64_t)n);
+#pragma unroll
+      for (int k = 0; k < KK; ++k) {
+        bv[k][n] = B[o + jd.b.ktab[k]] * fb;
+        bl[k][n] = Blo ? Blo[o + jd.b.ktab[k]] * fb : 0.f;
+      }
+    }
+    uint32_t bits = 0;
+#pragma unroll
+    for (int i = 0; i < U; ++i) {
+      float av[4][KK];
+      if constexpr (KFAST) {
+        // one run of 4*KK values: element r of the run is m = r / KK, k = r % KK
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int k = 0; k < KK; ++k) av[q][k] = f4_at(x[i][(q * KK + k) >> 2], (q * KK + k) & 3) * fa;
+      } else {
+#pragma unroll
+        for (int k = 0; k < KK; ++k) {
+          av[0][k] = x[i][k].x * fa; av[1][k] = x[i][k].y * fa; av[2][k] = x[i][k].z * fa; av[3][k] = x[i][k].w * fa;
+        }
+      }
+      float out[4 * NN];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int n = 0; n < NN; ++n) {
+          float f = 0.f;
+          if (Blo) {
+#pragma unroll
+            for (int k = 0; k < KK; ++k) f = fmaf(av[q][k], bl[k][n], f);
+          }
+#pragma unroll
+          for (int k = 0; k < KK; ++k) f = fmaf(av[q][k], bv[k][n], f);
+          out[q * NN + n] = f;
+          bits = max(bits, __float_as_uint(f));
+        }
+      const uint64_t m0 = (q0 + (uint64_t)(lane + 32 * i)) << 2;
+      float* c = C + ((int64_t)b << mnb) + (int64_t)m0 * NN;
+#pragma unroll
+      for (int v = 0; v < NN; ++v)
+        reinterpret_cast<float4*>(c)[v] = make_float4(out[4 * v], out[4 * v + 1], out[4 * v + 2], out[4 * v + 3]);
+    }
+    // The whole warp is in slice b: one maximum per block.
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, off));
+    if (lane == 0) {
+      atomicMax(&jd.c_max[b], bits);
+      if (q0 == 0) jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - sa - sb;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Fused slice-invariant joins (OnceList).  Operands written earlier in the
 // same launch by other CTAs are read through L2 (ld.global.cg): L1 is not
@@ -1470,9 +1570,41 @@ bool stream_ok(int mode, const JoinDesc& jd, bool& kfast) {
   return true;
 }
 
+// k_stream_blk for one (KK, NN): U = 2^LOGU quads per lane, one warp per
+// block of 32*U quads, at most 16 CTAs per SM walking the blocks.
+template <int KK, int NN, int LOGU>
+void launch_stream_blk(const JoinDesc& jd, bool kfast, const int64_t* s0, int nslices, cudaStream_t st) {
+  const int64_t warps = (int64_t)nslices << (jd.mb - 7 - LOGU);
+  const int64_t ctas = (warps + kThreads / 32 - 1) / (kThreads / 32);
+  const int64_t cap = (int64_t)sm_count() * 16;
+  const int g = (int)(ctas < cap ? ctas : cap);
+  if (kfast) k_stream_blk<KK, NN, true, LOGU><<<g, kThreads, 0, st>>>(jd, s0, nslices);
+  else k_stream_blk<KK, NN, false, LOGU><<<g, kThreads, 0, st>>>(jd, s0, nslices);
+}
+
 bool launch_stream(int mode, const JoinDesc& jd, const int64_t* s0, int nslices, cudaStream_t st) {
   bool kfast = false;
   if (!stream_ok(mode, jd, kfast)) return false;
+  // Slices of at least one warp block (32 lanes x U quads): the block variant,
+  // four quads per lane (two when K = 4 or N >= 8, which hold more values).
+  const int logu = (jd.kb >= 2 || jd.nb >= 3) ? 1 : 2;
+  if (jd.mb >= 7 + logu) {
+    switch (jd.kb * 8 + jd.nb) {
+      case 0: launch_stream_blk<1, 1, 2>(jd, false, s0, nslices, st); return true;
+      case 1: launch_stream_blk<1, 2, 2>(jd, false, s0, nslices, st); return true;
+      case 2: launch_stream_blk<1, 4, 2>(jd, false, s0, nslices, st); return true;
+      case 3: launch_stream_blk<1, 8, 1>(jd, false, s0, nslices, st); return true;
+      case 4: launch_stream_blk<1, 16, 1>(jd, false, s0, nslices, st); return true;
+      case 8: launch_stream_blk<2, 1, 2>(jd, kfast, s0, nslices, st); return true;
+      case 9: launch_stream_blk<2, 2, 2>(jd, kfast, s0, nslices, st); return true;
+      case 10: launch_stream_blk<2, 4, 2>(jd, kfast, s0, nslices, st); return true;
+      case 11: launch_stream_blk<2, 8, 1>(jd, kfast, s0, nslices, st); return true;
+      case 16: launch_stream_blk<4, 1, 1>(jd, kfast, s0, nslices, st); return true;
+      case 17: launch_stream_blk<4, 2, 1>(jd, kfast, s0, nslices, st); return true;
+      case 18: launch_stream_blk<4, 4, 1>(jd, kfast, s0, nslices, st); return true;
+      default: break;
+    }
+  }
   const int64_t quads = (int64_t)nslices << (jd.mb - 2);
   const int g = grid_for(quads);
 #define TOGB_STREAM(KK, NN)                                                                \

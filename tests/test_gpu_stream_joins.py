@@ -86,6 +86,11 @@ CASES = [
     (6, 14, 1, 3, 2, "xy", "kfast"), (2, 12, 0, 4, 2, "xy", "mfast"),
     (0, 12, 1, 2, 3, "y", "mfast"), (13, 12, 1, 2, 2, "y", "kfast"), (4, 14, 1, 3, 3, "y", "kfast"),
     (1, 13, 2, 1, 2, "y", "mfast"), (3, 12, 0, 4, 2, "y", "mfast"),
+    # fewer than 32 x U quads of m per slice: the per-quad kernel (the cases
+    # above have enough for the warp-block kernel)
+    (0, 8, 1, 2, 0, "xy", "mfast"), (3, 8, 1, 2, 0, "xy", "kfast"), (0, 7, 2, 1, 0, "xy", "mfast"),
+    (44, 7, 2, 1, 0, "xy", "kfast"), (0, 6, 0, 3, 0, "xy", "mfast"), (12, 8, 2, 2, 0, "xy", "kfast"),
+    (2, 7, 1, 3, 0, "xy", "mfast"),
 ]
 
 
