@@ -68,6 +68,9 @@ struct JoinDesc {
   Runs r_inv_m, r_inv_n;  // output address bits -> m / n bits (inverse deposit of c_s_m / c_s_n)
   int32_t* err;        // device error word: set to 1 when a bounded wait gives up (may be null)
   int64_t wait_cycles; // SM clock cycles a pipeline wait may last before the kernel gives up
+  int32_t c_direct;    // tensor-core epilogue: store each row's 16-byte vectors straight from
+                       // registers instead of through shared-memory staging (host's choice)
+  int32_t pad_;
 };
 
 // Root reduction: adds every slice's root tensor into the compensated FP64

@@ -575,6 +575,40 @@ bool make_tmap(const OpDesc& o, int nslices, uint32_t box_rows, CUtensorMap* out
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Tensor-core epilogue of a row-major tile (the output's two lowest n bits are
+// its two lowest address bits): 1 when each lane should store its own row's
+// 16-byte vectors rather than transposing through shared memory.  Counts the
+// 128-byte lines one warp's stores of rows 0..31 x columns 0..31 touch both
+// ways; the staged path costs about four times the instructions, so the direct
+// path is taken while it touches at most twice the lines.
+int choose_direct_epilogue(const JoinDesc& jd) {
+  if (jd.nb < 2 || jd.c_s_n[0] != 1 || jd.c_s_n[1] != 2) return 0;
+  auto dep_bits = [](const int64_t* s, int nbits, int x) {
+    int64_t off = 0;
+    for (int i = 0; i < nbits; ++i)
+      if ((x >> i) & 1) off += s[i];
+    return off;
+  };
+  const int rows = std::min(32, 1 << jd.mb), cols = std::min(32, 1 << jd.nb);
+  int64_t direct = 0, staged = 0;
+  for (int j = 0; j < cols; j += 4) {  // direct: instruction j stores column group j of every row
+    std::vector<int64_t> lines;
+    for (int r = 0; r < rows; ++r) lines.push_back((dep_bits(jd.c_s_m, jd.mb, r) + dep_bits(jd.c_s_n, jd.nb, j)) / 32);
+    std::sort(lines.begin(), lines.end());
+    direct += std::unique(lines.begin(), lines.end()) - lines.begin();
+  }
+  for (int k = 0; k < rows / 4; ++k) {  // staged: instruction k stores four rows of eight vectors
+    std::vector<int64_t> lines;
+    for (int l = 0; l < 32; ++l) {
+      const int r = (l >> 3) + 4 * k, c = 4 * (l & 7);
+      if (r < rows && c < cols) lines.push_back((dep_bits(jd.c_s_m, jd.mb, r) + dep_bits(jd.c_s_n, jd.nb, c)) / 32);
+    }
+    std::sort(lines.begin(), lines.end());
+    staged += std::unique(lines.begin(), lines.end()) - lines.begin();
+  }
+  return direct <= 2 * staged ? 1 : 0;
+}
+
 // C = A.B^T computed as (B.A^T)^T: exchange the operands and the output's m/n strides.
 void swap_operands(JoinDesc& jd) {
   std::swap(jd.a, jd.b);
@@ -622,6 +656,7 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
       // The tensor-core kernel tiles 128 rows of M: put the larger extent there.
       if (split_kernel(p, J) == togb::K_UMMA) {
         if (jd.mb < 7 && jd.nb > jd.mb) swap_operands(jd);
+        jd.c_direct = choose_direct_epilogue(jd);
         const int sl_a = jd.a.batch_stride ? B : 1, sl_b = jd.b.batch_stride ? B : 1;
         p->use_tma[j] = plain_k_major(jd.a) && plain_k_major(jd.b) && jd.kb >= 2 &&
                         make_tmap(jd.a, sl_a, 128, &p->tmaps[2 * j]) &&
@@ -1198,6 +1233,8 @@ togb_status togb_program_describe(togb_program* p, int mode, int32_t join, char*
     static const char* names[] = {"direct", "staged", "stream", "stream_kfast"};
     s += std::string(" variant ") + names[togb::direct_variant(mode, jd)];
   }
+  if (join_kernel(p, J, mode) == togb::K_UMMA && mode == TOGB_MODE_SPLIT)
+    s += std::string(" epilogue ") + (jd.c_direct ? "direct" : "staged");
   s += "\n";
   auto strides = [&](const char* name, const int64_t* v, int nb) {
     s += name;

@@ -30,8 +30,11 @@
 // lowest n bits are the output's two lowest address bits, every read-out warp
 // transposes its 32 rows through a private shared-memory area and stores
 // 16-byte vectors, four rows of eight per instruction (whole 128-byte row
-// segments when the first five n bits are contiguous); otherwise lanes store
-// their rows' columns directly (coalesced when the m bits are lowest).  The
+// segments when the first five n bits are contiguous) -- or, when the host
+// finds that consecutive rows lie close together in the output (c_direct),
+// each lane stores its own row's vectors without the staging round trip;
+// otherwise lanes store their rows' columns directly (coalesced when the m
+// bits are lowest).  The
 // layout planner orders a GEMM consumer's shared axes so that the larger of its
 // GEMM-shaped producers gets such a layout.
 // The slice maximum and exponent are recorded like in the other split-form
@@ -360,7 +363,19 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
         for (int j = 0; j < HALF; ++j)
           if (col0 + j < nlim) bits = max(bits, __float_as_uint(fmaxf(acc[j], 0.f)));
       }
-      if (rowmajor) {
+      if (rowmajor && jd.c_direct) {
+        // Each lane stores its own row's 16-byte vectors: the host chose this
+        // when consecutive rows lie close together in the output, so one
+        // instruction's 32 vectors fall in a few lines.
+        if (row < mlim) {
+          const int64_t crow = tCm[row];
+#pragma unroll
+          for (int j = 0; j < HALF; j += 4)
+            if (col0 + j < nlim)
+              *reinterpret_cast<float4*>(C + crow + tCn[col0 + j]) =
+                  make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
+        }
+      } else if (rowmajor) {
         // 32 columns at a time through this warp's staging area: each lane
         // writes its row's eight float4, then one store instruction covers four
         // rows of eight vectors -- whole 128-byte segments when the first five
