@@ -125,7 +125,10 @@ togb_status togb_program_info_get(const togb_program* prog, togb_program_info* i
  * work on it; running it does not.  Destroy with togb_program_destroy. */
 togb_status togb_program_create_host(const togb_program_desc* desc, togb_program** out);
 /* Text description of join `join` in `mode`: GEMM extents, kernel, operand
- * and output strides and their bit runs (host-only programs). */
+ * and output strides and their bit runs.  A host-only program is lowered for
+ * `mode` on demand; a device program is described as its last run in `mode`
+ * lowered it (TOGB_ERR_UNSUPPORTED before such a run), including whether the
+ * root's dot product is formed in its operand's epilogue. */
 togb_status togb_program_describe(togb_program* prog, int mode, int32_t join, char* buf, size_t n);
 
 /* Zero the device-side slice accumulator (compensated FP64 sum). */

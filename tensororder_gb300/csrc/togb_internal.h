@@ -71,6 +71,14 @@ struct JoinDesc {
   int32_t c_direct;    // tensor-core epilogue: store each row's 16-byte vectors straight from
                        // registers instead of through shared-memory staging (host's choice)
   int32_t pad_;
+  // Root fused into this tensor-core join (split form): instead of storing its
+  // output C, the epilogue forms sum C[a] * Y[a] over its tile (Y: the root's
+  // other operand, stored at the same addresses) and writes one FP64 partial
+  // per read-out warp and tile.  Null dot_y: the ordinary epilogue.
+  const float* dot_y;  // Y of slice 0 of the chunk
+  int64_t dot_y_bs;    // elements of Y between slices (0 when Y is shared by every slice)
+  double* dot_part;    // slice b's partials at dot_part + b * dot_part_bs, tile t's warp w at t * 8 + w
+  int64_t dot_part_bs;
 };
 
 // Root reduction: adds every slice's root tensor into the compensated FP64
@@ -79,6 +87,16 @@ struct RootDesc {
   OpDesc r;            // outer bits = root entries in reference order
   double* acc_sum;
   double* acc_comp;
+  // Fused root (a count whose dot product was formed in the epilogue of the
+  // tensor-core join producing its right operand): slice b's value is
+  // 2^(px_exp[b] + py_exp[b * py_step]) times the sum, in order, of the npart
+  // FP64 partials at part + b * part_stride.  Null part: read the root tensor.
+  const double* part;
+  int64_t part_stride;
+  const int32_t* px_exp;
+  const int32_t* py_exp;
+  int32_t npart;
+  int32_t py_step;
 };
 
 namespace togb {
@@ -154,6 +172,8 @@ cudaError_t launch_umma_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUte
                            cudaStream_t st);
 // Rows of the B-operand TMA box of launch_umma_ws for an N of 2^nb.
 int umma_ws_box_rows_b(int nb);
+// log2 of the output tiles per slice launch_umma_ws cuts a 2^mb x 2^nb join into.
+int umma_ws_tile_bits(int mb, int nb);
 cudaError_t launch_set_s0(int64_t* d_s0, int64_t value, cudaStream_t st);
 // One leaf to materialise on the device (togb_program_create_compact).
 struct LeafBuild {

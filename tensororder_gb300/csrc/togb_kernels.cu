@@ -1337,11 +1337,20 @@ __global__ void __launch_bounds__(kThreads) k_root_tree(const __grid_constant__ 
   const int64_t oe = dep(rd.r.r_outer, (uint64_t)e);
   double sum = 0.0, comp = 0.0;
   for (int b = threadIdx.x; b < nslices; b += kThreads) {
-    const int64_t o = slice_offset(rd.r, b, s0 + b) + oe;
-    double x = (double)R[o];
-    if (MODE == 1) {
-      if (rd.r.ptr_lo) x += (double)((const float*)rd.r.ptr_lo)[o];
-      x = ldexp(x, op_exp(rd.r, b));
+    double x;
+    if (rd.part) {
+      // fused root: the slice's partials in order, then its exponent
+      const double* P = rd.part + (int64_t)b * rd.part_stride;
+      double t = 0.0;
+      for (int i = 0; i < rd.npart; ++i) t += P[i];
+      x = ldexp(t, rd.px_exp[b] + rd.py_exp[(int64_t)b * rd.py_step]);
+    } else {
+      const int64_t o = slice_offset(rd.r, b, s0 + b) + oe;
+      x = (double)R[o];
+      if (MODE == 1) {
+        if (rd.r.ptr_lo) x += (double)((const float*)rd.r.ptr_lo)[o];
+        x = ldexp(x, op_exp(rd.r, b));
+      }
     }
     const double t = sum + x;
     comp += two_sum_err(sum, x, t);

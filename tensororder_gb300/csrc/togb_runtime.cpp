@@ -160,6 +160,7 @@ struct togb_program {
   int64_t* d_s0 = nullptr;
   int32_t* d_err = nullptr; // set by a kernel whose bounded wait expired
   int64_t wait_cycles = togb::kDefaultWaitCycles;  // limit of every device-side pipeline wait
+  int root_fused = -1;     // index into joins of a root dot product formed in its operand's epilogue
   void* own_ws = nullptr;
   size_t own_ws_bytes = 0;
   cudaStream_t cap_stream = nullptr;
@@ -619,6 +620,40 @@ void swap_operands(JoinDesc& jd) {
   jd.c_natural = 0;
 }
 
+// A count whose final join R = Y . X is a full dot product (scalar root), where
+// X -- the right operand, the join queued just before R -- runs on the
+// warp-specialised tensor-core kernel and both operands are stored in R's
+// k order (address = k): X's epilogue forms the dot product with Y instead of
+// storing X, R is not launched, and the root kernel sums X's per-tile
+// partials.  This saves writing X and reading X and Y again (split form).
+void fuse_root(togb_program* p, int mode) {
+  p->root_fused = -1;
+  if (mode != TOGB_MODE_SPLIT || p->host_only) return;
+  const Node& R = p->nodes[p->root];
+  if (R.leaf >= 0 || R.rank != 0) return;
+  const Node& X = p->nodes[R.right];
+  const Node& Y = p->nodes[R.left];
+  if (X.leaf >= 0 || Y.leaf >= 0 || !X.dep) return;
+  const int jr = R.join, jx = X.join;
+  if (split_kernel(p, X) != togb::K_UMMA || !p->use_tma[jx]) return;
+  const JoinDesc& dr = p->jds[jr];
+  if (dr.a.outer_bits != 0 || dr.b.outer_bits != 0 || dr.kb != X.rank || !dr.a.exp_ptr) return;
+  for (int i = 0; i < dr.kb; ++i)
+    if (dr.a.s_k[i] != pow2(i) || dr.b.s_k[i] != pow2(i)) return;
+  JoinDesc& dx = p->jds[jx];
+  dx.dot_y = (const float*)dr.a.ptr;
+  dx.dot_y_bs = dr.a.batch_stride;
+  dx.dot_part = (double*)dx.c_ptr;  // X's own slot (2^rank floats per slice) holds its partials
+  dx.dot_part_bs = dx.c_batch_stride / 2;
+  p->rd.part = dx.dot_part;
+  p->rd.part_stride = dx.dot_part_bs;
+  p->rd.npart = 8 << togb::umma_ws_tile_bits(dx.mb, dx.nb);  // tiles per slice x read-out warps
+  p->rd.px_exp = dx.c_exp;
+  p->rd.py_exp = dr.a.exp_ptr;
+  p->rd.py_step = dr.a.meta_step;
+  p->root_fused = jr;
+}
+
 void build_descs(togb_program* p, int mode, void* ws_v, int B) {
   p->once_segs_mode = -1;  // fused slice-invariant lists follow the descriptors
   p->once_segs.clear();
@@ -667,9 +702,11 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
   // Root: outer bits enumerate the reference axis order, last axis lowest.
   const Node& Rn = p->nodes[p->root];
   std::vector<int> ref_lsb(Rn.ref.rbegin(), Rn.ref.rend());
+  p->rd = RootDesc{};
   fill_operand(p, Rn, ref_lsb, {}, mode, ws, B, p->rd.r);
   p->rd.acc_sum = p->d_acc;
   p->rd.acc_comp = p->d_acc + pow2(Rn.rank);
+  fuse_root(p, mode);
   if (mode == TOGB_MODE_SPLIT) {
     const WsLayout w = ws_layout(p, mode, ws, B);
     p->d_max = w.per_max;
@@ -888,6 +925,7 @@ togb_status enqueue_phase(togb_program* p, int mode, bool once, int nb, cudaStre
   for (size_t i = 0; i < js.size(); ++i) {
     const int j = js[i];
     if (ev) TOGB_CUDA(cudaEventRecord((*ev)[i], st));
+    if (!once && j == p->root_fused) continue;  // formed in its right operand's epilogue
     const Node& J = p->nodes[p->joins[j]];
     const int kernel = join_kernel(p, J, mode);
     cudaError_t e;
@@ -1218,8 +1256,8 @@ togb_status togb_program_describe(togb_program* p, int mode, int32_t join, char*
   if (!p || !buf || n == 0) return fail(TOGB_ERR_INVALID, "null argument");
   if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
   if (join < 0 || join >= (int32_t)p->joins.size()) return fail(TOGB_ERR_INVALID, "join index out of range");
-  if (p->cur_mode != mode || !p->host_only) {
-    if (!p->host_only) return fail(TOGB_ERR_UNSUPPORTED, "describe works on host-only programs");
+  if (p->cur_mode != mode) {
+    if (!p->host_only) return fail(TOGB_ERR_UNSUPPORTED, "describe a device program after a run in this mode");
     // Descriptors against a null workspace: offsets are what matters here.
     build_descs(p, mode, nullptr, 1);
     p->cur_mode = mode;
@@ -1234,7 +1272,8 @@ togb_status togb_program_describe(togb_program* p, int mode, int32_t join, char*
     s += std::string(" variant ") + names[togb::direct_variant(mode, jd)];
   }
   if (join_kernel(p, J, mode) == togb::K_UMMA && mode == TOGB_MODE_SPLIT)
-    s += std::string(" epilogue ") + (jd.c_direct ? "direct" : "staged");
+    s += std::string(" epilogue ") + (jd.dot_y ? "root_dot" : (jd.c_direct ? "direct" : "staged"));
+  if (join == p->root_fused) s += " fused_into_operand";
   s += "\n";
   auto strides = [&](const char* name, const int64_t* v, int nb) {
     s += name;
@@ -1310,7 +1349,8 @@ togb_status togb_program_launch_count(const togb_program* p, int mode, int64_t* 
   }
   const int64_t B = p->cur_mode == mode && p->cur_B > 0 ? p->cur_B : p->num_slices;
   const int64_t chunks = (p->num_slices + B - 1) / B;
-  *launches = once + chunks * ((int64_t)p->per.size() + 2);
+  const int64_t fused = p->cur_mode == mode && p->root_fused >= 0 ? 1 : 0;
+  *launches = once + chunks * ((int64_t)p->per.size() - fused + 2);
   return TOGB_OK;
 }
 

@@ -96,6 +96,14 @@ struct TileMap {
 // The stage ring and the two accumulator sets run continuously across tiles,
 // so the next tile's loads, conversions and first MMAs overlap the current
 // tile's epilogue.
+// s[i] += x_i * y_i for the four lanes of a vector.
+__device__ __forceinline__ void fma4(const float4 x, const float4 y, float* s) {
+  s[0] = fmaf(x.x, y.x, s[0]);
+  s[1] = fmaf(x.y, y.y, s[1]);
+  s[2] = fmaf(x.z, y.z, s[2]);
+  s[3] = fmaf(x.w, y.w, s[3]);
+}
+
 template <int BN, int NR, int NC, bool PAIRS>
 __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant__ JoinDesc jd,
                                                           const __grid_constant__ CUtensorMap tmA,
@@ -355,8 +363,56 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
       if (__any_sync(0xffffffffu, *abort != 0)) break;  // warp-uniform
       const int mlim = (int)min((int64_t)kBM, M - (int64_t)m0);
       const int nlim = (int)min((int64_t)BN, N - (int64_t)n0);
-      float* __restrict__ C = (float*)jd.c_ptr + (int64_t)b * jd.c_batch_stride + deposit(jd.c_s_m, m0) +
-                              deposit(jd.c_s_n, n0);
+      // Fused root (dot): this join's output is consumed only by the count's
+      // final dot product with Y, stored at the same addresses.  Instead of
+      // storing, the epilogue reads Y at those addresses and forms the products
+      // in four FP32 chains per lane; the warp adds the lanes' sums in FP64 in
+      // a fixed order and writes one partial per warp and tile (the root kernel
+      // adds them in order: the same bits every run).
+      const bool dot = jd.dot_y != nullptr;
+      const int64_t at = (int64_t)b * (dot ? jd.dot_y_bs : jd.c_batch_stride) + deposit(jd.c_s_m, m0) +
+                         deposit(jd.c_s_n, n0);
+      float* __restrict__ C = (float*)jd.c_ptr + at;
+      const float* __restrict__ Y = jd.dot_y + at;
+      if (dot) {
+        // Y is read along the lane's own row, a batch of vectors at a time:
+        // every load of a batch is issued before the first product, so their
+        // latencies overlap (each 128-byte line is read whole by one lane).
+        float s4[4] = {0.f, 0.f, 0.f, 0.f};
+        if (row < mlim) {
+          const float* __restrict__ Yr = Y + tCm[row];
+          if (rowmajor) {
+#pragma unroll
+            for (int h = 0; h < HALF; h += 32) {
+              float4 y[8];
+#pragma unroll
+              for (int i = 0; i < 8; ++i)
+                y[i] = col0 + h + 4 * i < nlim ? __ldg(reinterpret_cast<const float4*>(Yr + tCn[col0 + h + 4 * i]))
+                                               : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+              for (int i = 0; i < 8; ++i)
+                fma4(make_float4(acc[h + 4 * i], acc[h + 4 * i + 1], acc[h + 4 * i + 2], acc[h + 4 * i + 3]), y[i], s4);
+            }
+          } else {
+#pragma unroll
+            for (int h = 0; h < HALF; h += 16) {
+              float y[16];
+#pragma unroll
+              for (int i = 0; i < 16; ++i) y[i] = col0 + h + i < nlim ? __ldg(Yr + tCn[col0 + h + i]) : 0.f;
+#pragma unroll
+              for (int i = 0; i < 16; ++i) s4[i & 3] = fmaf(acc[h + i], y[i], s4[i & 3]);
+            }
+          }
+        }
+        double d = ((double)s4[0] + (double)s4[1]) + ((double)s4[2] + (double)s4[3]);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
+        const int64_t tis = t & ((1ll << tm.tps_bits) - 1);  // tile within the slice
+        if (lane == 0) jd.dot_part[(int64_t)b * jd.dot_part_bs + tis * kReadWarps + (warp - 8)] = d;
+        if (m0 == 0 && n0 == 0 && rt == 0)
+          jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - op_shift(jd.a, b) - op_shift(jd.b, b);
+        continue;
+      }
       uint32_t bits = 0;
       if (row < mlim) {
 #pragma unroll
@@ -424,6 +480,7 @@ cudaError_t launch_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorM
   const int tm_bits = jd.mb > 7 ? jd.mb - 7 : 0;
   tm.tn_bits = jd.nb > bn_bits ? jd.nb - bn_bits : 0;
   tm.tps_bits = tm_bits + tm.tn_bits;
+  if (tm.tps_bits != umma_ws_tile_bits(jd.mb, jd.nb)) return cudaErrorInvalidValue;
   if (tm.tps_bits > 40) return cudaErrorInvalidValue;
   const int64_t ntiles = (int64_t)nslices << tm.tps_bits;
   const int64_t grid = ntiles < sm_count() ? ntiles : sm_count();
@@ -434,6 +491,11 @@ cudaError_t launch_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorM
 }  // namespace
 
 int umma_ws_box_rows_b(int nb) { return nb >= 7 ? 128 : 64; }
+
+int umma_ws_tile_bits(int mb, int nb) {
+  const int bn_bits = nb >= 7 ? 7 : 6;
+  return (mb > 7 ? mb - 7 : 0) + (nb > bn_bits ? nb - bn_bits : 0);
+}
 
 cudaError_t launch_umma_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorMap& tb, int nslices,
                            cudaStream_t st) {

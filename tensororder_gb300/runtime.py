@@ -364,6 +364,13 @@ class DeviceProgram:
         check(lib().togb_program_joins(self._h, int(mode), out.ctypes.data_as(_i32p), n))
         return out[:n]
 
+    def describe(self, mode, join):
+        """The library's description of join ``join`` in ``mode``: shape,
+        kernel, operand layouts (as the last run in ``mode`` lowered them)."""
+        buf = ctypes.create_string_buffer(8192)
+        check(lib().togb_program_describe(self._h, int(mode), int(join), buf, 8192))
+        return buf.value.decode()
+
     def launch_count(self, mode):
         """Kernel launches of one count in ``mode`` as the last run queued them."""
         out = ctypes.c_int64()

@@ -35,8 +35,9 @@ def run_both(prog, mode, slices=None):
         if launches is None:
             launches = dp.launch_count(mode)
     info = dp.info
+    root_fused = "fused_into_operand" in dp.describe(mode, int(info.num_joins) - 1)
     dp.close()
-    return out[0], out[1], info, launches
+    return out[0], out[1], info, launches, root_fused
 
 
 @pytest.mark.parametrize("name", SLICED)
@@ -44,7 +45,7 @@ def run_both(prog, mode, slices=None):
 def test_fused_once_phase_equals_unfused(name, mode, cuda):
     doc = load_golden(name)
     prog = Program.from_dict(doc["program"])
-    fused, unfused, info, _ = run_both(prog, mode)
+    fused, unfused, info, _, _ = run_both(prog, mode)
     assert info.num_joins_once > 0
     assert np.array_equal(fused, unfused)
     tol = 1e-12 if mode == runtime.MODE_F64 else 1e-6
@@ -55,12 +56,14 @@ def test_fused_once_phase_equals_unfused(name, mode, cuda):
 def test_fused_once_phase_equals_unfused_n220(mode, cuda):
     with gzip.open(os.path.join(ROOT, "tensororder_gb300", "plans", "wvc220_s10.json.gz"), "rt") as f:
         prog = Program.from_dict(json.load(f)["program"])
-    fused, unfused, info, launches = run_both(prog, mode, slices=8)
+    fused, unfused, info, launches, root_fused = run_both(prog, mode, slices=8)
     assert info.num_joins_once == 361
     assert np.array_equal(fused, unfused)
     # A count is the slice-invariant phase, then per chunk of slices the slice
-    # base, the per-slice joins and the root: the 361 slice-invariant joins
-    # are queued as a handful of launches.
-    per_chunk = int(info.num_launches) + 1
+    # base, the per-slice joins (less the root join when its dot product is
+    # formed in its operand's epilogue, split form) and the root: the 361
+    # slice-invariant joins are queued as a handful of launches.
+    assert root_fused == (mode == runtime.MODE_SPLIT)
+    per_chunk = int(info.num_launches) + 1 - int(root_fused)
     assert launches // per_chunk >= 1
     assert launches % per_chunk <= 4
