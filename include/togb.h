@@ -165,7 +165,7 @@ togb_status togb_program_launch_count(const togb_program* prog, int mode, int64_
  * togb_program_joins; -1 restores the default).  A kernel that cannot run the
  * join in that form -- the split form's leaf residuals are applied only by the
  * thread-per-output and reduction kernels, the tensor-core kernel needs
- * M, N >= 64 and K >= 4 -- is rejected with TOGB_ERR_UNSUPPORTED.  The count
+ * M, N >= 32 and K >= 4 -- is rejected with TOGB_ERR_UNSUPPORTED.  The count
  * does not depend on the choice beyond the form's tolerance; only the speed
  * does.  No counterpart in the reference (numpy_apis.py:42-43 always calls
  * np.tensordot). */

@@ -77,11 +77,15 @@ int log2_exact(int64_t v) {
 }
 
 // Kernel for a join in a given form.  Long-K joins with few outputs get the
-// CTA-per-output reduction; GEMM-sized joins the tiled kernel; the rest the
-// thread-per-output kernel.
+// CTA-per-output reduction; GEMM-sized joins (M, N >= 32, K >= 16) the tiled
+// kernel, with K-major operands requested from their producers; the rest the
+// thread-per-output kernel.  M or N of 32 leaves part of a tile empty, which
+// costs little: such joins are bound by their operand and output bytes, while
+// a thread-per-output kernel reading operands whose K and free bits are
+// interleaved wastes most of every sector it loads.
 int choose_kernel(int mb, int nb, int kb) {
   if (kb >= 12 && mb + nb <= 6) return togb::K_REDUCE;
-  if (mb >= 6 && nb >= 6 && kb >= 4) return togb::K_TILED;
+  if (mb >= 5 && nb >= 5 && kb >= 4) return togb::K_TILED;
   return togb::K_DIRECT;
 }
 
@@ -524,7 +528,7 @@ bool kernel_allowed(const togb_program* p, const Node& J, int mode, int kernel) 
     case togb::K_DIRECT: return true;
     case togb::K_REDUCE: return mb + nb <= 20;  // one CTA per output entry and slice
     case togb::K_TILED: return mode == TOGB_MODE_F64 || !leaf;
-    case togb::K_UMMA: return mode == TOGB_MODE_SPLIT && !leaf && mb >= 6 && nb >= 6 && kb >= 2;
+    case togb::K_UMMA: return mode == TOGB_MODE_SPLIT && !leaf && mb >= 5 && nb >= 5 && kb >= 2;
     default: return false;
   }
 }
@@ -1271,8 +1275,10 @@ togb_status togb_program_describe(togb_program* p, int mode, int32_t join, char*
     static const char* names[] = {"direct", "staged", "stream", "stream_kfast"};
     s += std::string(" variant ") + names[togb::direct_variant(mode, jd)];
   }
-  if (join_kernel(p, J, mode) == togb::K_UMMA && mode == TOGB_MODE_SPLIT)
+  if (join_kernel(p, J, mode) == togb::K_UMMA && mode == TOGB_MODE_SPLIT) {
     s += std::string(" epilogue ") + (jd.dot_y ? "root_dot" : (jd.c_direct ? "direct" : "staged"));
+    if (!p->host_only) s += p->use_tma[join] ? " loads tma" : " loads gather";
+  }
   if (join == p->root_fused) s += " fused_into_operand";
   s += "\n";
   auto strides = [&](const char* name, const int64_t* v, int nb) {

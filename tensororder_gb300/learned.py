@@ -264,7 +264,7 @@ def allowed_kernels_host(j: costmodel.JoinShape, mode: int) -> List[int]:
         out.append(1)
     if j.lm + j.ln <= 20:
         out.append(2)
-    if mode == runtime.MODE_SPLIT and not leaf and j.lm >= 6 and j.ln >= 6 and j.lk >= 2:
+    if mode == runtime.MODE_SPLIT and not leaf and j.lm >= 5 and j.ln >= 5 and j.lk >= 2:
         out.append(3)
     return out
 
