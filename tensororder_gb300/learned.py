@@ -185,7 +185,9 @@ def record_timings(program: Program, mode: int, kernels: Sequence[int] = KERNELS
                    device: int = 0, max_slices: Optional[int] = None) -> List[TimingRow]:
     """Per-launch device times of every join of ``program`` under each kernel
     it may run: one timed pass per kernel id (joins that cannot run it keep
-    their default kernel), the first ``max_slices`` slices in one chunk."""
+    their default kernel), the first ``max_slices`` slices in one chunk.  Id
+    -1 is a pass with every join on its default kernel, recorded under the id
+    of that kernel."""
     import torch
 
     dp = runtime.DeviceProgram(program, device)
@@ -194,6 +196,7 @@ def record_timings(program: Program, mode: int, kernels: Sequence[int] = KERNELS
     B = min(S, (ws.numel() - int(dp.info.workspace_fixed[mode])) // max(1, int(dp.info.workspace_per_slice[mode])))
     table = costmodel.join_table(program)
     allowed = dp.allowed_kernels(mode)
+    defaults = [int(x) for x in dp.joins(mode)[:, 3]]
     rows: List[TimingRow] = []
     dp.set_timing(True)
     for k in kernels:
@@ -205,8 +208,9 @@ def record_timings(program: Program, mode: int, kernels: Sequence[int] = KERNELS
         torch.cuda.synchronize(device)
         t = dp.join_times()
         for j, js in enumerate(table):
-            if k in allowed[j]:  # this join ran kernel k in this pass
-                rows.append(TimingRow(join_features(js, k, B if js.per_slice else 1, mode), float(t[j])))
+            if k < 0 or k in allowed[j]:  # this join ran kernel k (its default for -1) in this pass
+                kj = defaults[j] if k < 0 else k
+                rows.append(TimingRow(join_features(js, kj, B if js.per_slice else 1, mode), float(t[j])))
     for j in range(len(allowed)):
         dp.set_kernel(mode, j, -1)
     dp.close()
@@ -273,9 +277,13 @@ class Selector:
     """Chooses the slice set and kernels of a plan for one form."""
 
     def __init__(self, mode: int, model: Optional[LearnedCostModel] = None, flops_per_s: float = 1e14,
-                 bytes_per_s: float = 5e12, max_workspace_bytes: float = 64e9):
+                 bytes_per_s: float = 5e12, max_workspace_bytes: float = 64e9,
+                 kernels: Optional[Sequence[int]] = None):
+        """``kernels``: the kernel ids the model was trained on (default: all);
+        the learned choice for a join is made among those it may run."""
         self.mode = mode
         self.model = model
+        self.kernels = None if kernels is None else set(kernels)
         self.flops_per_s = flops_per_s
         self.bytes_per_s = bytes_per_s
         self.max_ws = max_workspace_bytes
@@ -284,18 +292,25 @@ class Selector:
         return int(max(1, min(S, self.max_ws // max(1.0, per_slice_bytes))))
 
     def predict_learned(self, program: Program, per_slice_bytes: float) -> Tuple[float, List[int]]:
+        """Predicted time of one count and the kernel of every join (-1: its
+        default).  Each join chooses among its default kernel and the kernels
+        the model was trained on that it may run."""
         S = program.num_slices
         B = self._chunk(per_slice_bytes, S)
         chunks = (S + B - 1) // B
+        hp = runtime.HostProgram(program)
+        defaults = [int(x) for x in hp.joins(self.mode)[:, 3]]
+        hp.close()
         total = 0.0
         kernels = []
-        for j in costmodel.join_table(program):
-            ks = allowed_kernels_host(j, self.mode)
+        for j, d in zip(costmodel.join_table(program), defaults):
+            ks = [d] + [k for k in allowed_kernels_host(j, self.mode)
+                        if k != d and (self.kernels is None or k in self.kernels)]
             nb = B if j.per_slice else 1
             feats = np.stack([join_features(j, k, nb, self.mode) for k in ks])
             ms = self.model.predict_ms(feats)
             i = int(np.argmin(ms))
-            kernels.append(ks[i])
+            kernels.append(-1 if i == 0 else ks[i])
             total += (chunks if j.per_slice else 1) * float(ms[i]) * 1e-3
         return total, kernels
 
