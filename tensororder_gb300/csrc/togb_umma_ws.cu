@@ -6,13 +6,15 @@
 // [1, 2), is split into hi = tf32_rn(v) and lo = tf32_rn(v - hi), and every
 // product is hi.hi + hi.lo + lo.hi (the dropped lo.lo term is ~2^-22).
 //
-// One CTA computes a 128 x BN output tile of one slice with four roles:
+// One CTA computes a 128 x BN output tile of one slice with four roles, over a
+// ring of NS stages, each a hi buffer and a lo buffer of [A | B] chunk rows:
 //   warp 0        TMA producer: loads the 32-wide K chunks of A and B (128-byte
-//                 swizzle) into a ring of NR raw stages;
-//   warps 2-7     converters: split each landed chunk into hi and lo buffers of
-//                 the same swizzled layout in a ring of NC converted stages,
-//                 releasing the raw stage at once, so the loads in flight are
-//                 not held up by the MMAs;
+//                 swizzle) into a stage's hi buffer once the MMAs of the chunk
+//                 it held have completed;
+//   warps 2-7     converters: split each landed chunk in place -- hi over the
+//                 loaded values, lo into the stage's lo buffer, same swizzled
+//                 layout -- so a stage costs no separate raw buffer and three
+//                 stages fit (the loads run up to two chunks ahead);
 //   warp 1        MMA issuer: one thread issues the tcgen05.mma of each chunk;
 //   warps 8-15    read-out: drain the tensor-memory accumulators into FP32
 //                 registers and run the epilogue.
@@ -57,14 +59,14 @@ namespace {
 
 constexpr int kWsThreads = 512;  // 16 warps
 
-template <int BN, int NR, int NC>
+template <int BN, int NS>
 struct WsSmem {
   static constexpr int A_BYTES = kBM * kBK * 4;
   static constexpr int B_BYTES = BN * kBK * 4;
-  static constexpr int RAW = A_BYTES + B_BYTES;  // TMA target: [A | B]
-  static constexpr int CONV = 2 * RAW;           // [hi: A | B][lo: A | B]
+  static constexpr int RAW = A_BYTES + B_BYTES;  // one chunk: [A | B]
+  static constexpr int CONV = 2 * RAW;           // a stage: [hi: A | B] (the TMA target) [lo: A | B]
   static constexpr int STG = 8 * 32 * 32 * 4;   // per read-out warp: 32 rows x 32 columns of staging
-  static constexpr int DYN = NR * RAW + NC * CONV + STG + 1024;
+  static constexpr int DYN = NS * CONV + STG + 1024;
   static_assert(DYN + 1536 <= 227 * 1024, "shared memory budget");
 };
 
@@ -104,12 +106,12 @@ __device__ __forceinline__ void fma4(const float4 x, const float4 y, float* s) {
   s[3] = fmaf(x.w, y.w, s[3]);
 }
 
-template <int BN, int NR, int NC, bool PAIRS>
+template <int BN, int NS, bool PAIRS>
 __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant__ JoinDesc jd,
                                                           const __grid_constant__ CUtensorMap tmA,
                                                           const __grid_constant__ CUtensorMap tmB,
                                                           int64_t ntiles, TileMap tm) {
-  using L = WsSmem<BN, NR, NC>;
+  using L = WsSmem<BN, NS>;
   constexpr int HALF = BN / 2;         // columns per read-out warp
   constexpr uint32_t kCols = 512;      // all of tensor memory (one CTA per SM)
   constexpr int NSETS = kCols / BN;    // accumulator sets in rotation
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
   constexpr int kConvWarps = kConv / 32;
   constexpr int kReadWarps = 8;
   extern __shared__ unsigned char dyn_raw[];
-  __shared__ __align__(8) uint64_t full[NR], rawfree[NR], conv[NC], cfree[NC], accf[NSETS], acce[NSETS], fin;
+  __shared__ __align__(8) uint64_t full[NS], conv[NS], cfree[NS], accf[NSETS], acce[NSETS], fin;
   __shared__ uint32_t tmem_sh;
   __shared__ int abort_sh;
   __shared__ int32_t tCm[kBM], tCn[BN];  // output offsets within a tile (< 2^31 per slice)
@@ -138,11 +140,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
   for (int i = tid; i < kBM; i += kWsThreads) tCm[i] = (int32_t)deposit(jd.c_s_m, i);
   for (int i = tid; i < BN; i += kWsThreads) tCn[i] = (int32_t)deposit(jd.c_s_n, i);
   if (tid == 0) {
-    for (int i = 0; i < NR; ++i) {
+    for (int i = 0; i < NS; ++i) {
       mbar_init(smem_u32(&full[i]), 1);
-      mbar_init(smem_u32(&rawfree[i]), kConvWarps);
-    }
-    for (int i = 0; i < NC; ++i) {
       mbar_init(smem_u32(&conv[i]), kConvWarps);
       mbar_init(smem_u32(&cfree[i]), 1);
     }
@@ -174,12 +173,13 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
         tm.decode(t, b, m0, n0, BN);
         const int asl = jd.a.batch_stride ? b : 0, bsl = jd.b.batch_stride ? b : 0;
         for (int c = 0; c < nchunks; ++c, ++gc) {
-          const int st = gc % NR, u = gc / NR;
-          if (gc >= NR && !mbar_wait_or_abort(smem_u32(&rawfree[st]), (u - 1) & 1, abort, jd.wait_cycles)) {
+          const int st = gc % NS, u = gc / NS;
+          // The stage is free once the MMAs of the chunk it held have completed.
+          if (gc >= NS && !mbar_wait_or_abort(smem_u32(&cfree[st]), (u - 1) & 1, abort, jd.wait_cycles)) {
             *abort = 1;
             break;
           }
-          const uint32_t dst = sbase + st * L::RAW;
+          const uint32_t dst = sbase + st * L::CONV;
           const uint32_t bar = smem_u32(&full[st]);
           mbar_expect_tx(bar, (uint32_t)L::RAW);
           tma_load_3d(dst, &tmA, bar, c * kBK, (int)m0, asl);
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
         }
       }
       if (*abort)  // loads still in flight must land before the CTA may exit
-        for (int c = max(0, gc - NR); c < gc; ++c) mbar_wait_bounded(smem_u32(&full[c % NR]), (c / NR) & 1);
+        for (int c = max(0, gc - NS); c < gc; ++c) mbar_wait_bounded(smem_u32(&full[c % NS]), (c / NS) & 1);
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------------- MMA issuer
@@ -197,10 +197,10 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
       int gc = 0, gw = 0;  // chunks and windows consumed by this CTA
       for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
         for (int c = 0; c < nchunks && ok; ++c, ++gc) {
-          const int st = gc % NC, u = gc / NC;
+          const int st = gc % NS, u = gc / NS;
           if (!mbar_wait_or_abort(smem_u32(&conv[st]), u & 1, abort, jd.wait_cycles)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t a_hi = sbase + NR * L::RAW + st * L::CONV, b_hi = a_hi + L::A_BYTES;
+          const uint32_t a_hi = sbase + st * L::CONV, b_hi = a_hi + L::A_BYTES;
           const uint32_t a_lo = a_hi + L::RAW, b_lo = a_lo + L::A_BYTES;
           {
             const int set = gw % NSETS;
@@ -253,16 +253,16 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
       tm.decode(t, b, m0, n0, BN);
       const float fa = pow2f(op_shift(jd.a, b)), fb = pow2f(op_shift(jd.b, b));
       for (int c = 0; c < nchunks; ++c, ++gc) {
-        const int rs = gc % NR, ru = gc / NR, cs = gc % NC, cu = gc / NC;
-        const bool got = mbar_wait_or_abort(smem_u32(&full[rs]), ru & 1, abort, jd.wait_cycles) &&
-                         (gc < NC || mbar_wait_or_abort(smem_u32(&cfree[cs]), (cu - 1) & 1, abort, jd.wait_cycles));
+        const int cs = gc % NS, cu = gc / NS;
+        const bool got = mbar_wait_or_abort(smem_u32(&full[cs]), cu & 1, abort, jd.wait_cycles);
         if (!__all_sync(0xffffffffu, got)) {  // warp-uniform exit
           *abort = 1;
           ok = false;
           break;
         }
-        const unsigned char* raw = smem + rs * L::RAW;
-        unsigned char* hi = smem + NR * L::RAW + cs * L::CONV;
+        // In place: each thread reads its 16-byte pieces of the loaded chunk and
+        // writes hi over them and lo into the stage's lo buffer.
+        unsigned char* hi = smem + cs * L::CONV;
         unsigned char* lo = hi + L::RAW;
         // 16-byte pieces of a row the chunk's MMA k-steps read (two per k-step
         // of 8); the rest (K past the end) is neither read nor converted.
@@ -271,14 +271,12 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
         for (int e = ct; e < L::RAW / 16; e += kConv) {
           // 128-byte swizzle: piece p of row r holds logical piece p ^ (r % 8)
           if (live < 8 && (((e & 7) ^ ((e >> 3) & 7)) >= live)) continue;
-          const float4 x = *reinterpret_cast<const float4*>(raw + e * 16);
+          const float4 x = *reinterpret_cast<const float4*>(hi + e * 16);
           float4 h, l;
           split4(x, e * 16 < L::A_BYTES ? fa : fb, h, l);
           *reinterpret_cast<float4*>(hi + e * 16) = h;
           *reinterpret_cast<float4*>(lo + e * 16) = l;
         }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(smem_u32(&rawfree[rs]));  // raw stage read: the next load may land there
         fence_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_u32(&conv[cs]));
@@ -294,7 +292,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
     // two lowest address bits (four columns form one 16-byte vector); the
     // vectors of a row are then placed through the column offset table.
     const bool rowmajor = jd.nb >= 2 && jd.c_s_n[0] == 1 && jd.c_s_n[1] == 2;
-    float4* wst = reinterpret_cast<float4*>(smem + NR * L::RAW + NC * L::CONV) + (warp - 8) * 256;  // 32 rows x 8 float4
+    float4* wst = reinterpret_cast<float4*>(smem + NS * L::CONV) + (warp - 8) * 256;  // 32 rows x 8 float4
     int gw = 0;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
       int b;
@@ -469,11 +467,11 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
   if (tid == 0 && abort_sh && jd.err) atomicExch(jd.err, 1);
 }
 
-template <int BN, int NR, int NC, bool PAIRS>
+template <int BN, int NS, bool PAIRS>
 cudaError_t launch_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorMap& tb, int nslices,
                       cudaStream_t st) {
-  using L = WsSmem<BN, NR, NC>;
-  cudaError_t e = cudaFuncSetAttribute(k_umma_ws<BN, NR, NC, PAIRS>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::DYN);
+  using L = WsSmem<BN, NS>;
+  cudaError_t e = cudaFuncSetAttribute(k_umma_ws<BN, NS, PAIRS>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::DYN);
   if (e != cudaSuccess) return e;
   constexpr int bn_bits = BN == 128 ? 7 : 6;
   TileMap tm;
@@ -484,7 +482,7 @@ cudaError_t launch_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUtensorM
   if (tm.tps_bits > 40) return cudaErrorInvalidValue;
   const int64_t ntiles = (int64_t)nslices << tm.tps_bits;
   const int64_t grid = ntiles < sm_count() ? ntiles : sm_count();
-  k_umma_ws<BN, NR, NC, PAIRS><<<(unsigned)grid, kWsThreads, L::DYN, st>>>(jd, ta, tb, ntiles, tm);
+  k_umma_ws<BN, NS, PAIRS><<<(unsigned)grid, kWsThreads, L::DYN, st>>>(jd, ta, tb, ntiles, tm);
   return cudaGetLastError();
 }
 
@@ -501,9 +499,10 @@ cudaError_t launch_umma_ws(const JoinDesc& jd, const CUtensorMap& ta, const CUte
                            cudaStream_t st) {
   // More than 32 windows of 32 (K > 1024): the paired read-out.
   const bool pairs = jd.kb > 10;
+  // Three stages of 64 KB (BN = 128) or four of 48 KB (BN = 64).
   if (jd.nb >= 7)
-    return pairs ? launch_ws<128, 2, 2, true>(jd, ta, tb, nslices, st) : launch_ws<128, 2, 2, false>(jd, ta, tb, nslices, st);
-  return pairs ? launch_ws<64, 4, 2, true>(jd, ta, tb, nslices, st) : launch_ws<64, 4, 2, false>(jd, ta, tb, nslices, st);
+    return pairs ? launch_ws<128, 3, true>(jd, ta, tb, nslices, st) : launch_ws<128, 3, false>(jd, ta, tb, nslices, st);
+  return pairs ? launch_ws<64, 4, true>(jd, ta, tb, nslices, st) : launch_ws<64, 4, false>(jd, ta, tb, nslices, st);
 }
 
 }  // namespace togb
