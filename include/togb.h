@@ -117,6 +117,22 @@ typedef struct {
 togb_status togb_program_create_compact(const togb_program_desc* desc, const togb_leaf_spec* specs, int device,
                                         togb_program** out);
 
+/* New leaf values for a program made by togb_program_create_compact, for
+ * counting the same network again with other weights: specs[i] describes
+ * leaf i (same kind as at creation; clause polarities and variable weights may
+ * change) and dense_values the dense leaves' values in leaf order
+ * (num_dense_values of them).  The copies and the device build of clause and
+ * variable leaves are queued on `stream`; runs queued after them on that
+ * stream see the new leaves.  The lowering, layouts and workspaces are kept;
+ * when a leaf's power-of-two normaliser changes, the descriptors and captured
+ * graphs are rebuilt at the next run.  Validation as at creation:
+ * TOGB_ERR_INVALID for a changed kind or a wrong value count,
+ * TOGB_ERR_UNSUPPORTED for negative or non-finite values.  No counterpart in
+ * the reference, which rebuilds its tensors for every count
+ * (tensor_network_constructions.py:69-152). */
+togb_status togb_program_set_leaves(togb_program* prog, const togb_leaf_spec* specs, const double* dense_values,
+                                    int64_t num_dense_values, void* stream);
+
 togb_status togb_program_info_get(const togb_program* prog, togb_program_info* info);
 
 /* Lower and plan a program on the host only (no device, no leaf values

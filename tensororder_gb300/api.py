@@ -48,11 +48,16 @@ class GB300API:
     # device rate for sizing the first call before any has been timed (FLOP/s)
     _first_call_rate = {runtime.MODE_F64: 1.0e12, runtime.MODE_SPLIT: 5.0e13}
 
+    # Keep the last lowered program: a later count of the same network (same
+    # tree, slice groups, leaf axes and kinds) only uploads its leaves.
+    cache_programs = True
+
     def __init__(self, mode=runtime.MODE_F64, device=0):
         self._mode = mode
         self._device = device
         self._thread_limit = None
         self.last_program = None
+        self._cached = None  # (structure key, DeviceProgram)
 
     # -- configuration (numpy_apis.py:13-34) --------------------------------
     def add_argument(self, key, value):
@@ -146,12 +151,38 @@ class GB300API:
             if time.perf_counter() - t0 > 2e-3:
                 time.sleep(2e-4)
 
+    @staticmethod
+    def _structure_key(prog):
+        """What the lowering depends on: the tree, the slice groups and every
+        leaf's axes and kind (clause, variable or dense) -- not the weights."""
+        def kind(l):
+            return 1 if (l.kind == "or" and l.rank <= 30) else (2 if l.kind == "var" else 0)
+        return (tuple(prog.postorder), tuple(tuple(g) for g in prog.slice_groups),
+                tuple((kind(l), tuple(l.axes)) for l in prog.leaves))
+
+    def _program(self, prog, stream):
+        """The device program for ``prog``: the cached one with ``prog``'s
+        leaves uploaded when the structure matches, else a new one."""
+        if not self.cache_programs:
+            return runtime.DeviceProgram(prog, self._device)
+        key = self._structure_key(prog)
+        if self._cached is not None and self._cached[0] == key:
+            dp = self._cached[1]
+            dp.set_leaves(prog, stream)
+            return dp
+        if self._cached is not None:  # release its device memory before lowering the next
+            self._cached[1].close()
+            self._cached = None
+        dp = runtime.DeviceProgram(prog, self._device)
+        self._cached = (key, dp)
+        return dp
+
     def _run(self, prog, num_slice_limit):
         n = prog.num_slices if num_slice_limit is None else min(prog.num_slices, int(num_slice_limit))
         try:
-            dp = runtime.DeviceProgram(prog, self._device)
-            self.last_program = dp
             stream = self._stream()
+            dp = self._program(prog, stream)
+            self.last_program = dp
             dp.reset(stream)
             ws = dp.allocate_workspace(self._mode, max(n, 1))
             # First call sized from the FLOP count, later ones from the measured

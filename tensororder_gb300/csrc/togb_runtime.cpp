@@ -150,6 +150,7 @@ struct togb_program {
   std::vector<std::vector<int>> leaf_axes;
   std::vector<int64_t> leaf_off;
   std::vector<int> leaf_shift;  // split mode normaliser per leaf
+  std::vector<int> leaf_kind;   // togb_leaf_kind of each leaf as created
   double* d_leaf64 = nullptr;
   float* d_leaf32 = nullptr;    // split mode: FP32 rounding of each leaf value
   float* d_leaf32lo = nullptr;  // split mode: value - hi, rounded to FP32
@@ -167,6 +168,12 @@ struct togb_program {
   int root_fused = -1;     // index into joins of a root dot product formed in its operand's epilogue
   void* own_ws = nullptr;
   size_t own_ws_bytes = 0;
+  // togb_program_set_leaves: device build records and host staging, kept
+  // with the program so the copies queued on the caller's stream outlive it.
+  togb::LeafBuild* d_items = nullptr;
+  size_t d_items_cap = 0;
+  std::vector<togb::LeafBuild> h_items;
+  std::vector<float> h_hi, h_lo;
   cudaStream_t cap_stream = nullptr;
   // descriptors for the current (mode, chunk, workspace)
   int cur_mode = -1;
@@ -1009,6 +1016,34 @@ namespace {
 
 // Host half of togb_program_create: validation, lowering and planning.  No
 // device memory is touched.  Leaf values are validated only when present.
+// Split-form normaliser of one leaf: the power of two that brings its largest
+// entry into [1, 2) (0 for an all-zero leaf).  `vals` holds a dense leaf's
+// 2^r entries.  Returns an error message for values the forms cannot take.
+const char* leaf_normaliser(int kind, const togb_leaf_spec* spec, const double* vals, int r, int* shift) {
+  double mx = 0;
+  if (kind == TOGB_LEAF_VARIABLE) {
+    const double wn = spec->w_neg, wp = spec->w_pos;
+    if (!(wn >= 0) || !(wp >= 0) || std::isinf(wn) || std::isinf(wp))
+      return "variable weights must be finite and non-negative";
+    mx = r == 0 ? wn + wp : std::max(wn, wp);
+  } else if (kind == TOGB_LEAF_CLAUSE) {
+    if (spec->output_index >= r) return "clause output axis out of range";
+    mx = 1.0;
+  } else if (kind == TOGB_LEAF_DENSE) {
+    for (int64_t i = 0; vals && i < pow2(r); ++i) {
+      const double v = vals[i];
+      if (!(v >= 0) || std::isinf(v)) return "leaf entries must be finite and non-negative";
+      mx = std::max(mx, v);
+    }
+  } else {
+    return "unknown leaf kind";
+  }
+  int e2 = 0;
+  if (mx > 0) std::frexp(mx, &e2);  // mx in [2^(e2-1), 2^e2)
+  *shift = mx > 0 ? 1 - e2 : 0;
+  return nullptr;
+}
+
 togb_status lower_host(const togb_program_desc* d, int device, togb_program** out, int64_t* num_values,
                        const togb_leaf_spec* specs = nullptr) {
   if (!d || !out) return fail(TOGB_ERR_INVALID, "null argument");
@@ -1036,6 +1071,7 @@ togb_status lower_host(const togb_program_desc* d, int device, togb_program** ou
   p->leaf_axes.resize(d->num_leaves);
   p->leaf_off.resize(d->num_leaves);
   p->leaf_shift.resize(d->num_leaves);
+  p->leaf_kind.resize(d->num_leaves);
   int64_t ax = 0, voff = 0, dense_off = 0;
   for (int l = 0; l < d->num_leaves; ++l) {
     const int r = d->leaf_rank[l];
@@ -1043,37 +1079,19 @@ togb_status lower_host(const togb_program_desc* d, int device, togb_program** ou
     p->leaf_axes[l].assign(d->leaf_axes + ax, d->leaf_axes + ax + r);
     ax += r;
     p->leaf_off[l] = voff;
-    double mx = 0;
     const int kind = specs ? specs[l].kind : TOGB_LEAF_DENSE;
-    if (kind == TOGB_LEAF_VARIABLE) {
-      const double wn = specs[l].w_neg, wp = specs[l].w_pos;
-      if (!(wn >= 0) || !(wp >= 0) || std::isinf(wn) || std::isinf(wp)) {
-        delete p;
-        return fail(TOGB_ERR_UNSUPPORTED, "variable weights must be finite and non-negative");
-      }
-      mx = r == 0 ? wn + wp : std::max(wn, wp);
-    } else if (kind == TOGB_LEAF_CLAUSE) {
-      if (specs[l].output_index >= r) { delete p; return fail(TOGB_ERR_INVALID, "clause output axis out of range"); }
-      mx = 1.0;
-    } else if (kind == TOGB_LEAF_DENSE) {
-      const double* vals = d->leaf_values ? d->leaf_values + (specs ? dense_off : voff) : nullptr;
+    p->leaf_kind[l] = kind;
+    const double* vals = nullptr;
+    if (kind == TOGB_LEAF_DENSE) {
+      vals = d->leaf_values ? d->leaf_values + (specs ? dense_off : voff) : nullptr;
       if (specs && !vals) { delete p; return fail(TOGB_ERR_INVALID, "dense leaf without values"); }
-      for (int64_t i = 0; vals && i < pow2(r); ++i) {
-        const double v = vals[i];
-        if (!(v >= 0) || std::isinf(v)) {
-          delete p;
-          return fail(TOGB_ERR_UNSUPPORTED, "leaf entries must be finite and non-negative");
-        }
-        mx = std::max(mx, v);
-      }
       dense_off += pow2(r);
-    } else {
-      delete p;
-      return fail(TOGB_ERR_INVALID, "unknown leaf kind");
     }
-    int e2 = 0;
-    if (mx > 0) std::frexp(mx, &e2);  // mx in [2^(e2-1), 2^e2)
-    p->leaf_shift[l] = mx > 0 ? 1 - e2 : 0;
+    if (const char* why = leaf_normaliser(kind, specs ? &specs[l] : nullptr, vals, r, &p->leaf_shift[l])) {
+      delete p;
+      const bool bad = kind == TOGB_LEAF_CLAUSE || kind < 0 || kind > TOGB_LEAF_VARIABLE;
+      return fail(bad ? TOGB_ERR_INVALID : TOGB_ERR_UNSUPPORTED, why);
+    }
     voff += pow2(r);
   }
   // Post-order walk (TensorNetwork.identify).
@@ -1242,6 +1260,86 @@ togb_status togb_program_create_compact(const togb_program_desc* d, const togb_l
     return cuda_fail(e, "leaf build");
   }
   *out = p;
+  return TOGB_OK;
+}
+
+togb_status togb_program_set_leaves(togb_program* p, const togb_leaf_spec* specs, const double* dense_values,
+                                    int64_t num_dense_values, void* stream) {
+  if (!p || !specs) return fail(TOGB_ERR_INVALID, "null argument");
+  if (p->host_only) return fail(TOGB_ERR_UNSUPPORTED, "host-only program: it has no leaves on a device");
+  const int n = (int)p->leaf_rank.size();
+  int64_t want = 0;
+  for (int l = 0; l < n; ++l) {
+    if (specs[l].kind != p->leaf_kind[l]) return fail(TOGB_ERR_INVALID, "leaf " + std::to_string(l) + " changed kind");
+    if (specs[l].kind == TOGB_LEAF_DENSE) want += pow2(p->leaf_rank[l]);
+  }
+  if (num_dense_values != want || (want > 0 && !dense_values))
+    return fail(TOGB_ERR_INVALID, "dense leaf values: expected " + std::to_string(want));
+  // Validate everything and compute the normalisers before touching the device.
+  std::vector<int> shift(n);
+  int64_t dense_off = 0;
+  for (int l = 0; l < n; ++l) {
+    const int r = p->leaf_rank[l];
+    const double* vals = specs[l].kind == TOGB_LEAF_DENSE ? dense_values + dense_off : nullptr;
+    if (const char* why = leaf_normaliser(specs[l].kind, &specs[l], vals, r, &shift[l]))
+      return fail(specs[l].kind == TOGB_LEAF_CLAUSE ? TOGB_ERR_INVALID : TOGB_ERR_UNSUPPORTED, why);
+    if (vals) dense_off += pow2(r);
+  }
+  TOGB_CUDA(cudaSetDevice(p->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  // Dense leaves: FP64 values and their FP32 hi/lo split, staged in the program.
+  p->h_hi.resize((size_t)want);
+  p->h_lo.resize((size_t)want);
+  p->h_items.clear();
+  dense_off = 0;
+  for (int l = 0; l < n; ++l) {
+    const int r = p->leaf_rank[l];
+    if (specs[l].kind != TOGB_LEAF_DENSE) {
+      togb::LeafBuild it{};
+      it.off = p->leaf_off[l];
+      it.rank = r;
+      it.kind = specs[l].kind;
+      it.out_pos = specs[l].output_index >= 0 ? r - 1 - specs[l].output_index : -1;
+      for (int a = 0; a < r; ++a)
+        if (!((specs[l].positive >> a) & 1)) it.false_idx |= 1u << (r - 1 - a);
+      it.w_neg = specs[l].w_neg;
+      it.w_pos = specs[l].w_pos;
+      p->h_items.push_back(it);
+      continue;
+    }
+    const int64_t m = pow2(r), o = p->leaf_off[l];
+    const double* v = dense_values + dense_off;
+    for (int64_t i = 0; i < m; ++i) {
+      p->h_hi[dense_off + i] = (float)v[i];
+      p->h_lo[dense_off + i] = (float)(v[i] - (double)p->h_hi[dense_off + i]);
+    }
+    TOGB_CUDA(cudaMemcpyAsync(p->d_leaf64 + o, v, m * 8, cudaMemcpyHostToDevice, st));
+    TOGB_CUDA(cudaMemcpyAsync(p->d_leaf32 + o, p->h_hi.data() + dense_off, m * 4, cudaMemcpyHostToDevice, st));
+    TOGB_CUDA(cudaMemcpyAsync(p->d_leaf32lo + o, p->h_lo.data() + dense_off, m * 4, cudaMemcpyHostToDevice, st));
+    dense_off += m;
+  }
+  if (!p->h_items.empty()) {
+    if (p->h_items.size() > p->d_items_cap) {
+      if (p->d_items) {
+        TOGB_CUDA(cudaStreamSynchronize(st));  // an earlier build may still read the records
+        cudaFree(p->d_items);
+        p->d_items = nullptr;
+        p->d_items_cap = 0;
+      }
+      TOGB_CUDA(cudaMalloc(&p->d_items, p->h_items.size() * sizeof(togb::LeafBuild)));
+      p->d_items_cap = p->h_items.size();
+    }
+    TOGB_CUDA(cudaMemcpyAsync(p->d_items, p->h_items.data(), p->h_items.size() * sizeof(togb::LeafBuild),
+                              cudaMemcpyHostToDevice, st));
+    const cudaError_t e =
+        togb::launch_build_leaves(p->d_items, (int)p->h_items.size(), p->d_leaf64, p->d_leaf32, p->d_leaf32lo, st);
+    if (e != cudaSuccess) return cuda_fail(e, "leaf build");
+  }
+  if (shift != p->leaf_shift) {  // the normalisers are part of the descriptors: rebuild them
+    p->leaf_shift = shift;
+    clear_graphs(p);
+    p->cur_mode = -1;
+  }
   return TOGB_OK;
 }
 
@@ -1508,6 +1606,7 @@ void togb_program_destroy(togb_program* p) {
   cudaFree(p->d_s0);
   cudaFree(p->d_err);
   for (void* b : p->once_bufs) cudaFree(b);
+  if (p->d_items) cudaFree(p->d_items);
   if (p->own_ws) cudaFree(p->own_ws);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   delete p;

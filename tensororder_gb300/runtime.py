@@ -93,7 +93,7 @@ EXPORTS = [
     "togb_mlp_param_count", "togb_mlp_scratch_floats", "togb_mlp_forward", "togb_mlp_loss_grad", "togb_mlp_adam",
     "togb_batch_create", "togb_batch_run", "togb_batch_results", "togb_batch_destroy",
     "togb_program_create_host", "togb_program_describe", "togb_program_create_compact",
-    "togb_program_launch_count", "togb_program_set_wait_limit",
+    "togb_program_launch_count", "togb_program_set_wait_limit", "togb_program_set_leaves",
 ]
 
 KERNEL_NAMES = {0: "direct", 1: "tiled", 2: "reduce", 3: "tensor"}
@@ -134,6 +134,7 @@ def lib():
     L.togb_program_launch_count.argtypes = [c_void, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
     L.togb_program_set_kernel.argtypes = [c_void, ctypes.c_int, ctypes.c_int32, ctypes.c_int32]
     L.togb_program_set_wait_limit.argtypes = [c_void, ctypes.c_int64]
+    L.togb_program_set_leaves.argtypes = [c_void, ctypes.POINTER(LeafSpec), _f64p, ctypes.c_int64, c_void]
     L.togb_program_kernel_allowed.argtypes = [c_void, ctypes.c_int, ctypes.c_int32, ctypes.c_int32, _i32p]
     L.togb_batch_create.argtypes = [ctypes.POINTER(c_void), ctypes.c_int32, ctypes.c_int, ctypes.POINTER(c_void),
                                     ctypes.POINTER(ctypes.c_size_t), ctypes.c_int32, ctypes.POINTER(c_void)]
@@ -282,6 +283,20 @@ class DeviceProgram:
         check(lib().togb_program_info_get(self._h, ctypes.byref(info)))
         self.info = info
         self._workspace = None
+
+    def set_leaves(self, program: Program, stream=None):
+        """Upload the leaves of ``program`` -- the same network with other
+        weights or clause polarities (leaf kinds, ranks, axes, tree and slice
+        groups equal to this program's) -- and build them on the device,
+        queued on ``stream``.  Only for programs created with
+        ``leaves="device"``."""
+        d = _Desc(program, values="dense")
+        n = 0 if d.values is None else int(d.values.size)
+        vals = d.values.ctypes.data_as(_f64p) if d.values is not None else None
+        check(lib().togb_program_set_leaves(self._h, d.specs, vals, n, _stream_handle(stream)))
+        self.program = program
+        self._d = d  # keeps the arrays alive while the copies are queued
+        self.h2d_bytes = (0 if d.values is None else d.values.nbytes * 2) + ctypes.sizeof(LeafSpec) * len(program.leaves)
 
     @property
     def _values(self):
