@@ -89,7 +89,7 @@ def test_gemm_join_sliced(shape, mode, tol, cuda):
 
 
 
-@pytest.mark.parametrize("m,n,k", [(8, 11, 9), (9, 10, 6), (7, 7, 12), (10, 10, 4), (10, 9, 3)])
+@pytest.mark.parametrize("m,n,k", [(8, 11, 9), (9, 10, 6), (7, 7, 12), (10, 10, 4)])
 def test_tensor_core_join_mean_error(m, n, k, cuda):
     """The tensor cores truncate their FP32 accumulation, so a tensor-core
     join's outputs are low on average: by 1.0e-7 (relative, mean over all
