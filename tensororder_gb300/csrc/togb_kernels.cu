@@ -470,8 +470,8 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
   }
 }
 
-// Streaming variant for joins of a long operand A with a tiny B (N*K <= 16,
-// split form, A without a leaf residual): C[m][n] = sum_k A[m][k] * B[n][k]
+// Streaming variant for joins of a long operand A with a tiny B (K <= 4 with
+// N*K <= 16, or K = 8 with N = 1; split form, A without a leaf residual): C[m][n] = sum_k A[m][k] * B[n][k]
 // with C row-major (natural).  A's two lowest m bits are either its two lowest
 // address bits (KFAST false: each k gives one 16-byte vector of four
 // consecutive m) or lie directly above all of its k bits (KFAST true: four
@@ -1554,7 +1554,9 @@ bool launch_staged(int mode, const JoinDesc& jd, const int64_t* s0, int nslices,
 // one vector per k or one run with every k, every base offset 16-byte aligned.
 // Returns true when launched.
 bool stream_ok(int mode, const JoinDesc& jd, bool& kfast) {
-  if (mode != 1 || !jd.c_natural || jd.mb < 2 || jd.kb > 2 || jd.a.ptr_lo) return false;
+  // K <= 4, or K = 8 against a single column (N = 1).
+  if (mode != 1 || !jd.c_natural || jd.mb < 2 || jd.kb > 3 || (jd.kb == 3 && jd.nb > 0) || jd.a.ptr_lo)
+    return false;
   const int K = 1 << jd.kb, N = 1 << jd.nb;
   if (N * K > 16) return false;
   const OpDesc& a = jd.a;
@@ -1611,6 +1613,7 @@ bool launch_stream(int mode, const JoinDesc& jd, const int64_t* s0, int nslices,
       case 16: launch_stream_blk<4, 1, 1>(jd, kfast, s0, nslices, st); return true;
       case 17: launch_stream_blk<4, 2, 1>(jd, kfast, s0, nslices, st); return true;
       case 18: launch_stream_blk<4, 4, 1>(jd, kfast, s0, nslices, st); return true;
+      case 24: launch_stream_blk<8, 1, 1>(jd, kfast, s0, nslices, st); return true;
       default: break;
     }
   }
@@ -1634,6 +1637,7 @@ bool launch_stream(int mode, const JoinDesc& jd, const int64_t* s0, int nslices,
     case 16: TOGB_STREAM(4, 1) break;
     case 17: TOGB_STREAM(4, 2) break;
     case 18: TOGB_STREAM(4, 4) break;
+    case 24: TOGB_STREAM(8, 1) break;
     default: return false;
   }
 #undef TOGB_STREAM

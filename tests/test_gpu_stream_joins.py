@@ -1,7 +1,8 @@
 """Joins of a long intermediate with a tiny leaf -- the joins the split form
 runs on the streaming thread-per-quad kernel.  X (ranks 10-14) is the outer
 product of two seeded dense leaves; the root join contracts it with a dense
-leaf Y of at most 16 entries over k <= 2 shared edges.  The cases are chosen so
+leaf Y of at most 16 entries over k <= 2 shared edges (or k = 3 against a
+single free edge).  The cases are chosen so
 that X's two lowest m bits are either its two lowest address bits or lie just
 above its k bits (the two operand layouts the streaming kernel reads), which
 the host-only lowering confirms without a GPU.  Sliced cases put the slice
@@ -67,7 +68,7 @@ def stream_layout(prog, join):
             sk = [int(x) for x in t[2:]]
         if t[:2] == ["A", "leaf"]:
             a_lo = int(t[2]) == 1
-    if not natural or a_lo or kb > 2 or (1 << (nb + kb)) > 16 or mb < 2:
+    if not natural or a_lo or kb > 3 or (kb == 3 and nb > 0) or (1 << (nb + kb)) > 16 or mb < 2:
         return None
     K = 1 << kb
     if so[:2] == [1, 2]:
@@ -91,6 +92,10 @@ CASES = [
     (0, 8, 1, 2, 0, "xy", "mfast"), (3, 8, 1, 2, 0, "xy", "kfast"), (0, 7, 2, 1, 0, "xy", "mfast"),
     (44, 7, 2, 1, 0, "xy", "kfast"), (0, 6, 0, 3, 0, "xy", "mfast"), (12, 8, 2, 2, 0, "xy", "kfast"),
     (2, 7, 1, 3, 0, "xy", "mfast"),
+    # K = 8 against a single column (N = 1)
+    (0, 12, 3, 0, 0, "xy", "mfast"), (2, 13, 3, 0, 2, "xy", "mfast"), (0, 12, 3, 0, 2, "y", "mfast"),
+    (1, 8, 3, 0, 2, "xy", "mfast"), (1, 7, 3, 0, 0, "xy", "mfast"), (24, 7, 3, 0, 0, "xy", "kfast"),
+    (24, 7, 3, 0, 2, "y", "kfast"),
 ]
 
 
