@@ -170,6 +170,27 @@ def _stream_handle(stream):
     return ctypes.c_void_p(stream.cuda_stream)
 
 
+def _leaf_specs(leaves):
+    """togb_leaf_spec records of ``leaves`` and the dense leaves' values
+    (concatenated in leaf order, or None when no leaf is dense)."""
+    specs = (LeafSpec * max(1, len(leaves)))()
+    vals = []
+    for i, l in enumerate(leaves):
+        sp = specs[i]
+        if l.kind == "or" and l.rank <= 30:
+            sp.kind = LEAF_CLAUSE
+            sp.output_index = -1 if l.output_index is None else int(l.output_index)
+            sp.positive = sum(1 << a for a, pos in enumerate(l.positive) if pos)
+        elif l.kind == "var":
+            sp.kind = LEAF_VARIABLE
+            sp.w_neg, sp.w_pos = float(l.w_neg), float(l.w_pos)
+        else:
+            sp.kind = LEAF_DENSE
+            vals.append(l.parent().ravel())
+    values = np.ascontiguousarray(np.concatenate(vals), dtype=np.float64) if vals else None
+    return specs, values
+
+
 class _Desc:
     """A togb_program_desc with the arrays it points into kept alive.
 
@@ -186,21 +207,7 @@ class _Desc:
             vals = [l.parent().ravel() for l in leaves]
             self.values = np.ascontiguousarray(np.concatenate(vals) if vals else np.zeros(1), dtype=np.float64)
         elif values == "dense":
-            specs = (LeafSpec * max(1, len(leaves)))()
-            vals = []
-            for i, l in enumerate(leaves):
-                if l.kind == "or" and l.rank <= 30:
-                    specs[i].kind = LEAF_CLAUSE
-                    specs[i].output_index = -1 if l.output_index is None else int(l.output_index)
-                    specs[i].positive = sum(1 << a for a, pos in enumerate(l.positive) if pos)
-                elif l.kind == "var":
-                    specs[i].kind = LEAF_VARIABLE
-                    specs[i].w_neg, specs[i].w_pos = float(l.w_neg), float(l.w_pos)
-                else:
-                    specs[i].kind = LEAF_DENSE
-                    vals.append(l.parent().ravel())
-            self.specs = specs
-            self.values = np.ascontiguousarray(np.concatenate(vals), dtype=np.float64) if vals else None
+            self.specs, self.values = _leaf_specs(leaves)
         else:
             self.values = None
         self.tokens = np.array(program.postorder, dtype=np.int32)
@@ -290,13 +297,13 @@ class DeviceProgram:
         groups equal to this program's) -- and build them on the device,
         queued on ``stream``.  Only for programs created with
         ``leaves="device"``."""
-        d = _Desc(program, values="dense")
-        n = 0 if d.values is None else int(d.values.size)
-        vals = d.values.ctypes.data_as(_f64p) if d.values is not None else None
-        check(lib().togb_program_set_leaves(self._h, d.specs, vals, n, _stream_handle(stream)))
+        specs, values = _leaf_specs(program.leaves)
+        n = 0 if values is None else int(values.size)
+        vals = values.ctypes.data_as(_f64p) if values is not None else None
+        check(lib().togb_program_set_leaves(self._h, specs, vals, n, _stream_handle(stream)))
         self.program = program
-        self._d = d  # keeps the arrays alive while the copies are queued
-        self.h2d_bytes = (0 if d.values is None else d.values.nbytes * 2) + ctypes.sizeof(LeafSpec) * len(program.leaves)
+        self._leaf_data = (specs, values)  # kept alive while the copies are queued
+        self.h2d_bytes = (0 if values is None else values.nbytes * 2) + ctypes.sizeof(LeafSpec) * len(program.leaves)
 
     @property
     def _values(self):
