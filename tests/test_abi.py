@@ -75,3 +75,20 @@ def test_tensordot_rejects_bad_axes(lib):
     st = lib.togb_tensordot_f64(a, 2, a, 2, 1, axes.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                                 axes.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), a, None)
     assert st == runtime.ERR_INVALID
+
+
+def test_set_leaves_validates_before_touching_a_device(lib):
+    """togb_program_set_leaves: null arguments are invalid, and a host-only
+    program (no leaves on a device) is refused without any CUDA call."""
+    from tensororder_gb300.program import Leaf, Program
+
+    prog = Program([Leaf([0], "var", w_neg=0.4, w_pos=0.6), Leaf([0], "var", w_neg=0.5, w_pos=0.5)],
+                   [0, 1, -1]).validate()
+    hp = runtime.HostProgram(prog)
+    specs, values = runtime._leaf_specs(prog.leaves)
+    try:
+        assert lib.togb_program_set_leaves(None, specs, None, 0, None) == runtime.ERR_INVALID
+        assert lib.togb_program_set_leaves(hp._h, None, None, 0, None) == runtime.ERR_INVALID
+        assert lib.togb_program_set_leaves(hp._h, specs, None, 0, None) == runtime.ERR_UNSUPPORTED
+    finally:
+        hp.close()
