@@ -5,7 +5,9 @@
 1. Records per-launch timings of every kernel each join may run (the
    backend's own CUDA-event timing) on training programs:
    * config-2 style GEMM joins: two seeded dense intermediates contracted with
-     random extents (``tests``-independent generator below),
+     random extents (``tests``-independent generator below), small ones under
+     every kernel and large ones (M, N of 2^12..2^14, K of 2^8..2^12) on their
+     default kernels,
    * slice candidates of the n=220 weighted cubic vertex-cover plan,
    * instances of the 512-instance uneven batch.
 2. Trains the MLP (the package's own forward/backward/Adam kernels).
@@ -57,13 +59,19 @@ def load_workload(name):
     return Program.from_dict(doc["program"]), doc["reference"]["float64"]
 
 
-def training_rows(batch_instances=16, gemm_programs=16, seed=0):
+def training_rows(batch_instances=16, gemm_programs=16, big_gemm_programs=8, seed=0):
     rows = []
     rng = np.random.default_rng(seed)
     for i in range(gemm_programs):
         m, n, k = (int(x) for x in rng.integers(6, 12, size=3))
         k = int(rng.integers(2, 11))
         rows += learned.record_timings(gemm_program(1000 + i, m, n, k), MODE, repeats=2)
+    # Joins of the size n=300's plans hold (up to 2^28 outputs, K up to 2^12), on
+    # their default kernels only: the thread-per-output kernel would take minutes.
+    for i in range(big_gemm_programs):
+        m, n = (int(x) for x in rng.integers(12, 15, size=2))
+        k = int(rng.integers(8, 13))
+        rows += learned.record_timings(gemm_program(2000 + i, m, n, k), MODE, kernels=(-1,), repeats=2)
     p220, _ = load_workload("wvc220_s10")
     base = Program(p220.leaves, p220.postorder, [])
     for cand in costmodel.slice_candidates(base, 10, 12):
