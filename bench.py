@@ -393,6 +393,23 @@ def main():
                                "3xTF32 product" % (tf32_peak / 1e12),
                 "tensor_pipe_tflops": 3 * top_flops / (jt_split[top] * 1e-3) / 1e12,
                 "bf16_measured_tflops": peaks.get("bf16_tflops")}
+        # The resource that binds the tensor-core kernel: shared memory.  Every
+        # 32-wide K chunk of a 128 x BN tile moves seven chunk-sizes through it:
+        # the TMA write, the converters' read and their hi and lo writes, and
+        # the MMAs' reads (hi.lo, lo.hi, hi.hi: three operand pairs).
+        a, b = (nb, mb) if (mb < 7 and nb > mb) else (mb, nb)  # the kernel tiles 128 rows of the larger
+        bn = 128 if b >= 7 else 64
+        tiles = max(1, (1 << a) // 128) * max(1, (1 << b) // bn) * runs
+        chunks = tiles * ((max(1, k // 8) + 3) // 4)
+        smem_bytes = 7.0 * chunks * 4 * 32 * (128 + bn)
+        sm_mhz = clocks.summary().get("sm_mhz") or peaks.get("sm_max_mhz") or 2070.0
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        per_clk = smem_bytes / (jt_split[top] * 1e-3) / sms / (sm_mhz * 1e6)
+        roof["smem_roofline"] = {
+            "bytes_per_launch": smem_bytes, "achieved_bytes_per_clk_per_sm": per_clk,
+            "peak_bytes_per_clk_per_sm": 128.0, "frac": per_clk / 128.0, "sm_mhz": sm_mhz, "sms": sms,
+            "model": "7 x (128 + BN) x 32 x 4 bytes per K chunk of 32 per tile (TMA write, converter read, "
+                     "hi and lo writes, three MMA operand-pair reads); peak = 32 banks x 4 bytes per clock"}
     else:  # memory-bound CUDA-core kernels
         roof = {"bound": "hbm", "achieved": top_bytes / (jt_split[top] * 1e-3) / 1e9,
                 "peak": peaks.get("hbm_gbs") or 6800.0, "unit": "GB/s",
