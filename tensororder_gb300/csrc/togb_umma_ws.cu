@@ -94,10 +94,6 @@ struct TileMap {
   }
 };
 
-// Persistent: each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...
-// The stage ring and the two accumulator sets run continuously across tiles,
-// so the next tile's loads, conversions and first MMAs overlap the current
-// tile's epilogue.
 // s[i] += x_i * y_i for the four lanes of a vector.
 __device__ __forceinline__ void fma4(const float4 x, const float4 y, float* s) {
   s[0] = fmaf(x.x, y.x, s[0]);
@@ -106,6 +102,10 @@ __device__ __forceinline__ void fma4(const float4 x, const float4 y, float* s) {
   s[3] = fmaf(x.w, y.w, s[3]);
 }
 
+// Persistent: each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// The stage ring and the accumulator sets run continuously across tiles, so
+// the next tile's loads, conversions and first MMAs overlap the current
+// tile's epilogue.
 template <int BN, int NS, bool PAIRS>
 __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant__ JoinDesc jd,
                                                           const __grid_constant__ CUtensorMap tmA,
