@@ -411,12 +411,20 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_umma_ws(const __grid_constant
           jd.c_exp[b] = op_exp(jd.a, b) + op_exp(jd.b, b) - op_shift(jd.a, b) - op_shift(jd.b, b);
         continue;
       }
-      uint32_t bits = 0;
+      // Slice maximum of the row's entries: a running fmaxf from +0 (negative
+      // and NaN entries count as 0), whose IEEE bits order like its value.
+      float mx = 0.f;
       if (row < mlim) {
+        if (col0 + HALF <= nlim) {
 #pragma unroll
-        for (int j = 0; j < HALF; ++j)
-          if (col0 + j < nlim) bits = max(bits, __float_as_uint(fmaxf(acc[j], 0.f)));
+          for (int j = 0; j < HALF; ++j) mx = fmaxf(mx, acc[j]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < HALF; ++j)
+            if (col0 + j < nlim) mx = fmaxf(mx, acc[j]);
+        }
       }
+      uint32_t bits = __float_as_uint(mx);
       if (rowmajor && jd.c_direct) {
         // Each lane stores its own row's 16-byte vectors: the host chose this
         // when consecutive rows lie close together in the output, so one
