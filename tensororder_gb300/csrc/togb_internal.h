@@ -89,9 +89,12 @@ struct RootDesc {
   double* acc_comp;
   // Fused root (a count whose dot product was formed in the epilogue of the
   // tensor-core join producing its right operand): slice b's value is
-  // 2^(px_exp[b] + py_exp[b * py_step]) times the sum, in order, of the npart
-  // FP64 partials at part + b * part_stride.  Null part: read the root tensor.
-  const double* part;
+  // 2^(px_exp[b] + py_exp[b * py_step]) times the sum of the npart FP64
+  // partials at part + b * part_stride, which the root kernel then writes over
+  // the slice's first partial.  `done` counts the root kernel's finished CTAs
+  // (zero between launches).  Null part: read the root tensor.
+  double* part;
+  uint32_t* done;
   int64_t part_stride;
   const int32_t* px_exp;
   const int32_t* py_exp;

@@ -1337,20 +1337,11 @@ __global__ void __launch_bounds__(kThreads) k_root_tree(const __grid_constant__ 
   const int64_t oe = dep(rd.r.r_outer, (uint64_t)e);
   double sum = 0.0, comp = 0.0;
   for (int b = threadIdx.x; b < nslices; b += kThreads) {
-    double x;
-    if (rd.part) {
-      // fused root: the slice's partials in order, then its exponent
-      const double* P = rd.part + (int64_t)b * rd.part_stride;
-      double t = 0.0;
-      for (int i = 0; i < rd.npart; ++i) t += P[i];
-      x = ldexp(t, rd.px_exp[b] + rd.py_exp[(int64_t)b * rd.py_step]);
-    } else {
-      const int64_t o = slice_offset(rd.r, b, s0 + b) + oe;
-      x = (double)R[o];
-      if (MODE == 1) {
-        if (rd.r.ptr_lo) x += (double)((const float*)rd.r.ptr_lo)[o];
-        x = ldexp(x, op_exp(rd.r, b));
-      }
+    const int64_t o = slice_offset(rd.r, b, s0 + b) + oe;
+    double x = (double)R[o];
+    if (MODE == 1) {
+      if (rd.r.ptr_lo) x += (double)((const float*)rd.r.ptr_lo)[o];
+      x = ldexp(x, op_exp(rd.r, b));
     }
     const double t = sum + x;
     comp += two_sum_err(sum, x, t);
@@ -1373,6 +1364,59 @@ __global__ void __launch_bounds__(kThreads) k_root_tree(const __grid_constant__ 
     const double t = a + b;
     rd.acc_comp[e] += sc[0] + two_sum_err(a, b, t);
     rd.acc_sum[e] = t;
+  }
+}
+
+// The fused root: the count's slice values from the partials its operand's
+// tensor-core epilogue wrote.  A warp per slice adds the slice's partials
+// (lane-strided, then a fixed shuffle tree), applies the slice's exponents
+// and writes the value over the slice's first partial.  The last CTA to
+// finish (a device counter, no waiting) adds the slice values with
+// k_root_tree's compensated tree, adds the total into the accumulator and
+// resets the counter.  Every order is fixed: the same bits every run.
+__global__ void __launch_bounds__(kThreads) k_root_parts(const __grid_constant__ RootDesc rd, int nslices) {
+  __shared__ double ss[kThreads], sc[kThreads];
+  __shared__ int last;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.x * (kThreads / 32) + warp;
+  if (b < nslices) {
+    double* P = rd.part + (int64_t)b * rd.part_stride;
+    double t = 0.0;
+    for (int i = lane; i < rd.npart; i += 32) t += P[i];
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    if (lane == 0) P[0] = ldexp(t, rd.px_exp[b] + rd.py_exp[(int64_t)b * rd.py_step]);
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(rd.done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double sum = 0.0, comp = 0.0;
+  for (int s = threadIdx.x; s < nslices; s += kThreads) {
+    const double x = __ldcg(rd.part + (int64_t)s * rd.part_stride);
+    const double t = sum + x;
+    comp += two_sum_err(sum, x, t);
+    sum = t;
+  }
+  ss[threadIdx.x] = sum;
+  sc[threadIdx.x] = comp;
+  __syncthreads();
+  for (int w = kThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      const double a = ss[threadIdx.x], c = ss[threadIdx.x + w];
+      const double t = a + c;
+      sc[threadIdx.x] += sc[threadIdx.x + w] + two_sum_err(a, c, t);
+      ss[threadIdx.x] = t;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double a = rd.acc_sum[0], c = ss[0];
+    const double t = a + c;
+    rd.acc_comp[0] += sc[0] + two_sum_err(a, c, t);
+    rd.acc_sum[0] = t;
+    *rd.done = 0;
   }
 }
 
@@ -1745,6 +1789,10 @@ cudaError_t launch_once_list(int mode, const OnceList& ol, cudaStream_t st) {
 
 cudaError_t launch_root(int mode, const RootDesc& rd, const int64_t* s0, int nslices, cudaStream_t st) {
   const int64_t E = 1ll << rd.r.outer_bits;
+  if (rd.part) {  // fused root (a count): a warp per slice, the last CTA adds them up
+    k_root_parts<<<(unsigned)((nslices + kThreads / 32 - 1) / (kThreads / 32)), kThreads, 0, st>>>(rd, nslices);
+    return cudaGetLastError();
+  }
   if (E <= 1024) {  // few root entries: a CTA per entry, slices across its threads
     if (mode == 0) k_root_tree<0, double><<<(unsigned)E, kThreads, 0, st>>>(rd, s0, nslices);
     else k_root_tree<1, float><<<(unsigned)E, kThreads, 0, st>>>(rd, s0, nslices);

@@ -657,6 +657,7 @@ void fuse_root(togb_program* p, int mode) {
   dx.dot_part = (double*)dx.c_ptr;  // X's own slot (2^rank floats per slice) holds its partials
   dx.dot_part_bs = dx.c_batch_stride / 2;
   p->rd.part = dx.dot_part;
+  p->rd.done = reinterpret_cast<uint32_t*>(p->d_err + 1);
   p->rd.part_stride = dx.dot_part_bs;
   p->rd.npart = 8 << togb::umma_ws_tile_bits(dx.mb, dx.nb);  // tiles per slice x read-out warps
   p->rd.px_exp = dx.c_exp;
@@ -1175,8 +1176,8 @@ togb_status togb_program_create(const togb_program_desc* d, int device, togb_pro
       (e = cudaMalloc(&p->d_leaf32lo, std::max<int64_t>(voff, 1) * 4)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_acc, 2 * E * 8)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_s0, 8)) != cudaSuccess ||
-      (e = cudaMalloc(&p->d_err, 4)) != cudaSuccess ||
-      (e = cudaMemset(p->d_err, 0, 4)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_err, 8)) != cudaSuccess ||  // error word, root kernel's CTA counter
+      (e = cudaMemset(p->d_err, 0, 8)) != cudaSuccess ||
       (e = cudaMemcpy(p->d_leaf64, d->leaf_values, voff * 8, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(p->d_leaf32, v32.data(), voff * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(p->d_leaf32lo, v32lo.data(), voff * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -1222,8 +1223,8 @@ togb_status togb_program_create_compact(const togb_program_desc* d, const togb_l
       (e = cudaMalloc(&p->d_leaf32lo, std::max<int64_t>(voff, 1) * 4)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_acc, 2 * E * 8)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_s0, 8)) != cudaSuccess ||
-      (e = cudaMalloc(&p->d_err, 4)) != cudaSuccess ||
-      (e = cudaMemset(p->d_err, 0, 4)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_err, 8)) != cudaSuccess ||  // error word, root kernel's CTA counter
+      (e = cudaMemset(p->d_err, 0, 8)) != cudaSuccess ||
       (e = cudaMemset(p->d_acc, 0, 2 * E * 8)) != cudaSuccess ||
       (e = cudaMemset(p->d_s0, 0, 8)) != cudaSuccess ||
       (e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking)) != cudaSuccess ||
