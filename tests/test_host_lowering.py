@@ -47,3 +47,28 @@ def test_n220_slice_invariant_phase_is_two_launches(mode):
     launches, once, per_and_root = launch_plan(prog, mode)
     assert once == 361
     assert launches == 2 + per_and_root + 1
+
+
+@pytest.mark.parametrize("m,n,k,plain,split", [
+    (5, 14, 5, 1, 3), (14, 5, 5, 1, 3), (5, 5, 4, 1, 3), (6, 6, 4, 1, 3),  # GEMM-classed: M, N >= 32, K >= 16
+    (4, 14, 5, 0, 0), (5, 14, 3, 0, 0), (12, 2, 1, 0, 0),                   # thread-per-output
+])
+def test_gemm_classification(m, n, k, plain, split):
+    """A join of two intermediates is GEMM-classed when M, N >= 32 and K >= 16:
+    the plain form runs it on the tiled kernel (1), the split form on the
+    tensor cores (3); smaller ones stay on the thread-per-output kernel (0)."""
+    import sys
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from test_gpu_gemm_joins import make_program
+
+    prog = make_program(7 + m + n + k, m, n, k)
+    hp = runtime.HostProgram(prog)
+    try:
+        root = prog.num_joins - 1
+        got = (int(hp.joins(runtime.MODE_F64)[root][3]), int(hp.joins(runtime.MODE_SPLIT)[root][3]))
+        mnk = sorted((int(x) for x in hp.joins(runtime.MODE_SPLIT)[root][:2]))
+    finally:
+        hp.close()
+    assert mnk == sorted((m, n))
+    assert got == (plain, split)
