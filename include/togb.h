@@ -42,9 +42,15 @@ typedef enum {
 } togb_status;
 
 typedef enum {
-  TOGB_MODE_F64 = 0,  /* plain form: FP64 storage and arithmetic          */
-  TOGB_MODE_SPLIT = 1 /* chosen form: FP32 storage with a per-slice power-of-two
-                         exponent per tensor; FP64 only in the slice sum  */
+  TOGB_MODE_F64 = 0,   /* plain form: FP64 storage and arithmetic          */
+  TOGB_MODE_SPLIT = 1, /* chosen form: FP32 storage with a per-slice power-of-two
+                          exponent per tensor; FP64 only in the slice sum  */
+  TOGB_MODE_INT64 = 2  /* int form: 64-bit integer storage and arithmetic
+                          modulo 2^64, the reference's "int" and "uint"
+                          entry types (numpy int64 / uint64,
+                          src/tensor_network/tensor_apis/numpy_apis.py:15-22).
+                          Leaf values are converted toward zero.  Read the
+                          result with togb_program_result_u64.        */
 } togb_mode;
 
 typedef struct togb_program togb_program;
@@ -79,8 +85,8 @@ typedef struct {
   int32_t num_launches;          /* kernel launches per chunk of slices        */
   double flops_per_slice;        /* per-slice joins: sum of 2*M*N*K            */
   double bytes_per_slice_f64;    /* per-slice joins: sum of 8*(M*K + K*N + M*N) */
-  int64_t workspace_per_slice[2];/* workspace bytes per slice, by togb_mode    */
-  int64_t workspace_fixed[2];    /* workspace bytes independent of slice count */
+  int64_t workspace_per_slice[3];/* workspace bytes per slice, by togb_mode    */
+  int64_t workspace_fixed[3];    /* workspace bytes independent of slice count */
   int32_t num_joins_once;        /* slice-invariant joins                      */
   int32_t pad_;
   double flops_once;             /* slice-invariant joins: sum of 2*M*N*K      */
@@ -147,7 +153,10 @@ togb_status togb_program_create_host(const togb_program_desc* desc, togb_program
  * root's dot product is formed in its operand's epilogue. */
 togb_status togb_program_describe(togb_program* prog, int mode, int32_t join, char* buf, size_t n);
 
-/* Zero the device-side slice accumulator (compensated FP64 sum). */
+/* Zero the device-side slice accumulator (compensated FP64 sum, or the int
+ * form's words).  Runs between two resets must use forms of one kind: FP64
+ * and split runs add FP64 sums, int-form runs add 64-bit words
+ * (TOGB_ERR_INVALID otherwise). */
 togb_status togb_program_reset(togb_program* prog, void* stream);
 
 /* Contract slices [slice_begin, slice_end) in `mode` and add them into the
@@ -162,6 +171,12 @@ togb_status togb_program_run(togb_program* prog, int mode, int64_t slice_begin, 
  * entries, row-major in the reference's output axis order) to host `out`,
  * together with the compensation terms (`comp`, may be NULL). */
 togb_status togb_program_result(togb_program* prog, void* stream, double* out, double* comp, int64_t n);
+
+/* The int form's result: wait for `stream` and copy the accumulated root
+ * tensor (2^root_rank 64-bit words, the sums modulo 2^64; read them as int64
+ * or uint64) to host `out`.  TOGB_ERR_INVALID when the accumulator holds FP64
+ * sums. */
+togb_status togb_program_result_u64(togb_program* prog, void* stream, uint64_t* out, int64_t n);
 
 /* Per join in post-order, five int32: log2 M, log2 N, log2 K over unsliced
  * axes, the kernel used in `mode` (0 thread-per-output, 1 tiled SIMT GEMM,
@@ -250,7 +265,8 @@ togb_status togb_contract_static_f64(const togb_program_desc* desc, const double
  * into the caller's stream.  The programs' kernels (togb_program_set_kernel)
  * and workspaces are fixed when the batch is created; a program may belong
  * to one live batch at a time and must not be run on its own meanwhile.  The
- * reference contracts instances one after another (execution.py:122-152). */
+ * reference contracts instances one after another (execution.py:122-152).
+ * `mode` is TOGB_MODE_F64 or TOGB_MODE_SPLIT. */
 typedef struct togb_batch togb_batch;
 togb_status togb_batch_create(togb_program* const* progs, int32_t n, int mode, void* const* workspaces,
                               const size_t* workspace_bytes, int32_t nstreams, togb_batch** out);

@@ -10,6 +10,15 @@ and ``execution.py`` use it): ``add_argument``, ``get_entry_size``,
 * ``gb300-split`` -- chosen form: FP32 storage with per-slice power-of-two
   exponents, FP64 only in the compensated slice sum.
 
+``--entry_type`` picks the form as the reference's backends pick their dtype
+(``numpy_apis.py:13-27``, ``tensorflow_apis.py:64-80``): ``float64`` keeps the
+library's form, ``float32`` and ``float16`` take the split form (FP32 storage,
+at least float16's range and precision), ``int`` and ``uint`` take the int
+form (64-bit words, sums and products modulo 2^64, as numpy's int64 and
+uint64 tensors wrap; the count is a numpy int64 or uint64 scalar).
+``bigint`` (numpy object arrays) has no device form and is refused, as the
+reference's GPU backend refuses it.
+
 ``contract_sliced`` is the hot path.  It flattens the plan
 (:func:`tensororder_gb300.program.from_plan`), hands it to libtogb and runs the
 slices as a sequence of calls of bounded device time (about
@@ -41,12 +50,15 @@ _OOM = OutOfMemoryError
 
 
 class GB300API:
-    """Execution backend; ``mode`` is ``runtime.MODE_F64`` or ``runtime.MODE_SPLIT``."""
+    """Execution backend; ``mode`` is ``runtime.MODE_F64``, ``runtime.MODE_SPLIT``
+    or ``runtime.MODE_INT64``."""
 
     slices_per_call = 1 << 14  # upper bound on slices queued by one C call
     max_call_seconds = 0.25    # target device time of one call (timeout granularity)
     # device rate for sizing the first call before any has been timed (FLOP/s)
-    _first_call_rate = {runtime.MODE_F64: 1.0e12, runtime.MODE_SPLIT: 5.0e13}
+    _first_call_rate = {runtime.MODE_F64: 1.0e12, runtime.MODE_SPLIT: 5.0e13, runtime.MODE_INT64: 3.0e11}
+    # numpy type of the int form's count, by entry type
+    _word_types = {"int": np.int64, "uint": np.uint64}
 
     # Keep the last lowered program: a later count of the same network (same
     # tree, slice groups, leaf axes and kinds) only uploads its leaves.
@@ -54,6 +66,7 @@ class GB300API:
 
     def __init__(self, mode=runtime.MODE_F64, device=0):
         self._mode = mode
+        self._word_type = np.int64  # the int form's count type
         self._device = device
         self._thread_limit = None
         self.last_program = None
@@ -64,8 +77,12 @@ class GB300API:
         if key == "entry_type":
             if value == "float64":
                 return
-            if value == "float32":
+            if value in ("float32", "float16"):
                 self._mode = runtime.MODE_SPLIT
+                return
+            if value in self._word_types:
+                self._mode = runtime.MODE_INT64
+                self._word_type = self._word_types[value]
                 return
             raise ValueError("Unknown gb300 type %s" % value)
         if key == "thread_limit":
@@ -76,7 +93,7 @@ class GB300API:
         raise ValueError("Invalid argument " + str(key) + " for selected tensor_library")
 
     def get_entry_size(self):
-        return 8 if self._mode == runtime.MODE_F64 else 4
+        return 4 if self._mode == runtime.MODE_SPLIT else 8
 
     # -- tensor primitives ---------------------------------------------------
     def create_tensor(self, shape, default_value=None):
@@ -197,6 +214,8 @@ class GB300API:
                 self._wait(stream)
                 per_slice = (time.perf_counter() - t0) / (e - s)
                 s = e
+            if self._mode == runtime.MODE_INT64:
+                return dp.result_words(stream, self._word_type)
             return dp.result(stream)
         except runtime.DeviceOutOfMemory as exc:
             raise _OOM(str(exc))

@@ -190,6 +190,8 @@ struct LeafBuild {
 // Fill the FP64 values and the FP32 hi/lo split of every listed leaf.
 cudaError_t launch_build_leaves(const LeafBuild* items, int n, double* v64, float* v32, float* v32lo,
                                 cudaStream_t st);
+// The int form's leaf words: out[i] = the int64 value of v64[i] rounded toward zero.
+cudaError_t launch_leaf_int(const double* v64, void* out, int64_t n, cudaStream_t st);
 // out[e] = acc[e] + acc[E + e]: the compensated sum of a root accumulator.
 cudaError_t launch_finalize(const double* acc, int64_t E, double* out, cudaStream_t st);
 cudaError_t probe_peak(int kind, cudaStream_t st, double* flops);

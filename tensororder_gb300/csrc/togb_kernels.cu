@@ -40,6 +40,34 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// Element type of the int form: 64-bit words with wrapping (modulo 2^64)
+// arithmetic, which gives int64 and uint64 sums and products bit for bit.
+using u64 = unsigned long long;
+
+// The FP64 form's multiply-add is an FMA; the int form's wraps.
+__device__ __forceinline__ double mad(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ u64 mad(u64 a, u64 b, u64 c) { return a * b + c; }
+
+// 16-byte vector of an element type.
+template <class T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; };
+template <> struct Vec16<double> { using type = double2; };
+template <> struct Vec16<u64> { using type = ulonglong2; };
+
+// Wrapping sum of one word per thread over the CTA; the total in thread 0.
+// Every thread of the CTA must call it.
+__device__ __forceinline__ u64 block_sum_u64(u64 v) {
+  __shared__ u64 red[kThreads / 32];
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  u64 t = 0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+  return t;
+}
+
 // Dot product of one output over K.  KK > 0: K == KK <= 16, offsets from the
 // per-join table and every load issued before the FMAs; KK == 0: any K, offsets
 // advanced with the dk deltas.  Split form: inputs scaled by fa/fb (exact powers
@@ -72,7 +100,7 @@ __device__ __forceinline__ T dot_k(const JoinDesc& jd, const T* __restrict__ A, 
     } else {
       T acc = 0;
 #pragma unroll
-      for (int k = 0; k < KK; ++k) acc = fma(av[k], bv[k], acc);
+      for (int k = 0; k < KK; ++k) acc = mad(av[k], bv[k], acc);
       return acc;
     }
   } else {
@@ -102,7 +130,7 @@ __device__ __forceinline__ T dot_k(const JoinDesc& jd, const T* __restrict__ A, 
     } else {
       T acc = 0;
       for (int k = 0; k < K; ++k) {
-        acc = fma(A[oa + ka], B[ob + kb], acc);
+        acc = mad(A[oa + ka], B[ob + kb], acc);
         const int t = __ffs(~k) - 1;
         ka += jd.a.dk[t];
         kb += jd.b.dk[t];
@@ -118,6 +146,10 @@ __device__ __forceinline__ void store_vec(float* p, const float* v) {
 __device__ __forceinline__ void store_vec(double* p, const double* v) {
   reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
   reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+__device__ __forceinline__ void store_vec(u64* p, const u64* v) {
+  reinterpret_cast<ulonglong2*>(p)[0] = make_ulonglong2(v[0], v[1]);
+  reinterpret_cast<ulonglong2*>(p)[1] = make_ulonglong2(v[2], v[3]);
 }
 
 // Thread-per-output kernel: each thread computes VEC consecutive outputs in
@@ -257,7 +289,7 @@ __device__ __forceinline__ void lds_row(const T* __restrict__ p, T* v) {
         const float4 x = reinterpret_cast<const float4*>(p)[c];
         v[4 * c] = x.x; v[4 * c + 1] = x.y; v[4 * c + 2] = x.z; v[4 * c + 3] = x.w;
       } else {
-        const double2 x = reinterpret_cast<const double2*>(p)[c];
+        const typename Vec16<T>::type x = reinterpret_cast<const typename Vec16<T>::type*>(p)[c];
         v[2 * c] = x.x; v[2 * c + 1] = x.y;
       }
     }
@@ -452,7 +484,7 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
         } else {
           T acc = 0;
 #pragma unroll
-          for (int k = 0; k < KK; ++k) acc = fma(ar[k], br[k], acc);
+          for (int k = 0; k < KK; ++k) acc = mad(ar[k], br[k], acc);
           out[j] = acc;
         }
       }
@@ -749,7 +781,7 @@ __device__ __forceinline__ T once_dot(const OnceJoin& oj, int K, const T* av, co
     T acc = 0;
 #pragma unroll
     for (int k = 0; k < KMAX; ++k)
-      if (k < K) acc = fma(av[k], bv[k], acc);
+      if (k < K) acc = mad(av[k], bv[k], acc);
     return acc;
   }
 }
@@ -772,7 +804,7 @@ __device__ T once_dot_serial(const OnceJoin& oj, int64_t oa, int64_t ob, int K, 
     return (T)f;
   } else {
     T acc = 0;
-    for (int k = 0; k < K; ++k) acc = fma(__ldcg(A + oa + oj.a_ktab[k]), __ldcg(B + ob + oj.b_ktab[k]), acc);
+    for (int k = 0; k < K; ++k) acc = mad(__ldcg(A + oa + oj.a_ktab[k]), __ldcg(B + ob + oj.b_ktab[k]), acc);
     return acc;
   }
 }
@@ -801,7 +833,7 @@ __device__ T once_dot_long(const OnceJoin& oj, int64_t oa, int64_t ob, int K, fl
   } else {
     T acc = 0;
     for (int k = 0; k < K; ++k)
-      acc = fma(__ldcg(A + oa + dep(oj.a_k, (uint64_t)k)), __ldcg(B + ob + dep(oj.b_k, (uint64_t)k)), acc);
+      acc = mad(__ldcg(A + oa + dep(oj.a_k, (uint64_t)k)), __ldcg(B + ob + dep(oj.b_k, (uint64_t)k)), acc);
     return acc;
   }
 }
@@ -954,6 +986,10 @@ __device__ __forceinline__ void load4(const double* p, double* v) {
   const double2 x = reinterpret_cast<const double2*>(p)[0], y = reinterpret_cast<const double2*>(p)[1];
   v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
 }
+__device__ __forceinline__ void load4(const u64* p, u64* v) {
+  const ulonglong2 x = reinterpret_cast<const ulonglong2*>(p)[0], y = reinterpret_cast<const ulonglong2*>(p)[1];
+  v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
+}
 
 template <int MODE, class T>
 __global__ void __launch_bounds__(kThreads) k_tiled(const __grid_constant__ JoinDesc jd,
@@ -1036,7 +1072,7 @@ __global__ void __launch_bounds__(kThreads) k_tiled(const __grid_constant__ Join
       Bs[kk][i] = v;
     }
     __syncthreads();
-    if constexpr (MODE == 0) {
+    if constexpr (MODE != 1) {
 #pragma unroll
       for (int kk = 0; kk < BK; ++kk) {
         T av[4], bv[4];
@@ -1045,7 +1081,7 @@ __global__ void __launch_bounds__(kThreads) k_tiled(const __grid_constant__ Join
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+          for (int j = 0; j < 4; ++j) acc[i][j] = mad(av[i], bv[j], acc[i][j]);
       }
     } else {
       T part[4][4];
@@ -1135,9 +1171,27 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const __grid_constant__ Joi
   int64_t pa8 = 0, pb8 = 0;
   for (int i = 0; i < LOGT && i < jd.kb; ++i) { pa8 += jd.a.s_k[i]; pb8 += jd.b.s_k[i]; }
   const int64_t steps = (jd.kb > LOGT) ? (1ll << (jd.kb - LOGT)) : (tid < (1 << jd.kb) ? 1 : 0);
+  if constexpr (MODE == 2) {  // int form: a wrapping sum, no compensation
+    u64 sum = 0;
+    constexpr int U = 4;
+    for (int64_t j0 = 0; j0 < steps; j0 += U) {
+      u64 y[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        y[u] = (j0 + u < steps) ? A[ka] * B[kb] : 0ull;
+        const int t8 = __ffsll(~(unsigned long long)(j0 + u)) - 1 + LOGT;
+        if (t8 < TOGB_MAXBITS) { ka += jd.a.dk[t8] + pa8; kb += jd.b.dk[t8] + pb8; }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) sum += y[u];
+    }
+    const u64 total = block_sum_u64(sum);
+    if (tid == 0) ((T*)jd.c_ptr)[(int64_t)b * jd.c_batch_stride + dep(jd.r_cm, m) + dep(jd.r_cn, n)] = total;
+    return;
+  }
   int sa = 0, sb = 0;
   double hi = 0.0, lo = 0.0;
-  if (MODE == 1) {
+  if constexpr (MODE == 1) {
     sa = op_shift(jd.a, b);
     sb = op_shift(jd.b, b);
     const float fa = pow2f(sa), fb = pow2f(sb);
@@ -1219,7 +1273,7 @@ template <int MODE, class T>
 __global__ void __launch_bounds__(kThreads) k_reduce_vec(const __grid_constant__ JoinDesc jd,
                                                          const int64_t* __restrict__ d_s0, int nslices) {
   constexpr int VW = 16 / sizeof(T);  // elements per vector
-  using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  using V = typename Vec16<T>::type;
   __shared__ double red_hi[kThreads / 32];
   __shared__ double red_lo[kThreads / 32];
   const int mnb = jd.mb + jd.nb;
@@ -1262,11 +1316,20 @@ __global__ void __launch_bounds__(kThreads) k_reduce_vec(const __grid_constant__
       const T* x = reinterpret_cast<const T*>(&av[u]);
       const T* y = reinterpret_cast<const T*>(&bv[u]);
 #pragma unroll
-      for (int q = 0; q < VW; ++q) part = fma(x[q] * fa, y[q] * fb, part);
+      for (int q = 0; q < VW; ++q) part = mad(x[q] * fa, y[q] * fb, part);
     }
-    const T t = sum + part;
-    comp += fabs(sum) >= fabs(part) ? (sum - t) + part : (part - t) + sum;
-    sum = t;
+    if constexpr (MODE == 2) {
+      sum += part;
+    } else {
+      const T t = sum + part;
+      comp += fabs(sum) >= fabs(part) ? (sum - t) + part : (part - t) + sum;
+      sum = t;
+    }
+  }
+  if constexpr (MODE == 2) {  // int form: a wrapping sum over the CTA
+    const u64 total = block_sum_u64(sum);
+    if (tid == 0) ((T*)jd.c_ptr)[(int64_t)b * jd.c_batch_stride + dep(jd.r_cm, m) + dep(jd.r_cn, n)] = total;
+    return;
   }
   double hi = (double)sum, lo = (double)comp;
   for (int off = 16; off > 0; off >>= 1) {
@@ -1289,28 +1352,38 @@ __global__ void __launch_bounds__(kThreads) k_reduce_vec(const __grid_constant__
 }
 
 // Compensated (Neumaier) accumulation of every slice's root tensor, in slice
-// order, into the FP64 accumulator.
+// order, into the FP64 accumulator (the int form adds wrapping words).
 template <int MODE, class T>
 __global__ void k_root(const __grid_constant__ RootDesc rd, const int64_t* __restrict__ d_s0, int nslices) {
   const int64_t E = 1ll << rd.r.outer_bits;
   const int64_t s0 = d_s0 ? *d_s0 : 0;
   const T* __restrict__ R = (const T*)rd.r.ptr;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
-    double sum = rd.acc_sum[e], comp = rd.acc_comp[e];
-    const int64_t oe = dep(rd.r.r_outer, (uint64_t)e);
-    for (int b = 0; b < nslices; ++b) {
-      const int64_t o = slice_offset(rd.r, b, s0 + b) + oe;
-      double x = (double)R[o];
-      if (MODE == 1) {
-        if (rd.r.ptr_lo) x += (double)((const float*)rd.r.ptr_lo)[o];
-        x = ldexp(x, op_exp(rd.r, b));
-      }
-      const double t = sum + x;
-      if (fabs(sum) >= fabs(x)) comp += (sum - t) + x; else comp += (x - t) + sum;
-      sum = t;
+  if constexpr (MODE == 2) {  // int form: the accumulator's sums are wrapping words
+    u64* acc = reinterpret_cast<u64*>(rd.acc_sum);
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+      u64 sum = acc[e];
+      const int64_t oe = dep(rd.r.r_outer, (uint64_t)e);
+      for (int b = 0; b < nslices; ++b) sum += R[slice_offset(rd.r, b, s0 + b) + oe];
+      acc[e] = sum;
     }
-    rd.acc_sum[e] = sum;
-    rd.acc_comp[e] = comp;
+  } else {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+      double sum = rd.acc_sum[e], comp = rd.acc_comp[e];
+      const int64_t oe = dep(rd.r.r_outer, (uint64_t)e);
+      for (int b = 0; b < nslices; ++b) {
+        const int64_t o = slice_offset(rd.r, b, s0 + b) + oe;
+        double x = (double)R[o];
+        if (MODE == 1) {
+          if (rd.r.ptr_lo) x += (double)((const float*)rd.r.ptr_lo)[o];
+          x = ldexp(x, op_exp(rd.r, b));
+        }
+        const double t = sum + x;
+        if (fabs(sum) >= fabs(x)) comp += (sum - t) + x; else comp += (x - t) + sum;
+        sum = t;
+      }
+      rd.acc_sum[e] = sum;
+      rd.acc_comp[e] = comp;
+    }
   }
 }
 
@@ -1335,6 +1408,13 @@ __global__ void __launch_bounds__(kThreads) k_root_tree(const __grid_constant__ 
   const int64_t s0 = d_s0 ? *d_s0 : 0;
   const T* __restrict__ R = (const T*)rd.r.ptr;
   const int64_t oe = dep(rd.r.r_outer, (uint64_t)e);
+  if constexpr (MODE == 2) {  // int form: a wrapping sum, added into the accumulator's word
+    u64 isum = 0;
+    for (int b = threadIdx.x; b < nslices; b += kThreads) isum += R[slice_offset(rd.r, b, s0 + b) + oe];
+    const u64 total = block_sum_u64(isum);
+    if (threadIdx.x == 0) reinterpret_cast<u64*>(rd.acc_sum)[e] += total;
+    return;
+  }
   double sum = 0.0, comp = 0.0;
   for (int b = threadIdx.x; b < nslices; b += kThreads) {
     const int64_t o = slice_offset(rd.r, b, s0 + b) + oe;
@@ -1451,6 +1531,13 @@ __global__ void k_build_leaves(const LeafBuild* __restrict__ items, double* __re
   }
 }
 
+// The int form's leaves: each FP64 leaf value converted toward zero, the
+// conversion numpy applies when a float is stored into an int64 tensor.
+__global__ void k_leaf_int(const double* __restrict__ v64, u64* __restrict__ out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (u64)__double2ll_rz(v64[i]);
+}
+
 __global__ void k_finalize(const double* __restrict__ acc, int64_t E, double* __restrict__ out) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x)
     out[e] = acc[e] + acc[E + e];
@@ -1497,7 +1584,7 @@ __global__ void __launch_bounds__(kThreads) k_probe_dmma(double* out, int iters)
 // An operand k_reduce_vec can read: unit-stride K, no leaf residual, and every
 // possible base offset (slice, outer index) and the pointer 16-byte aligned.
 bool reduce_vec_ok(const OpDesc& o, int mode) {
-  const int64_t vw = mode == 0 ? 2 : 4;
+  const int64_t vw = mode == 1 ? 4 : 2;
   if (o.ptr_lo) return false;
   if (o.r_k.n != 1 || o.r_k.src[0] != 0 || o.r_k.dst[0] != 0) return false;
   if (((uintptr_t)o.ptr & 15) != 0 || o.batch_stride % vw != 0) return false;
@@ -1538,7 +1625,7 @@ bool staged_plan(int mode, const JoinDesc& jd, int nslices, StageInfo& si, size_
   const int mnb = jd.mb + jd.nb;
   if (jd.kb > 4 || mnb < 10) return false;
   const int K = 1 << jd.kb;
-  const size_t es = mode == 0 ? 8 : 4;
+  const size_t es = mode == 1 ? 4 : 8;
   bool found = false;
   StageInfo best{};
   size_t best_bytes = 0;
@@ -1580,6 +1667,7 @@ bool launch_staged(int mode, const JoinDesc& jd, const int64_t* s0, int nslices,
 #define TOGB_STAGED(KK)                                                                                    \
   {                                                                                                        \
     if (mode == 0) staged_launch(k_direct_staged<0, double, KK>, jd, si, s0, nslices, tiles, bytes, st);   \
+    else if (mode == 2) staged_launch(k_direct_staged<2, u64, KK>, jd, si, s0, nslices, tiles, bytes, st); \
     else staged_launch(k_direct_staged<1, float, KK>, jd, si, s0, nslices, tiles, bytes, st);              \
   }
   switch (jd.kb) {
@@ -1729,6 +1817,7 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
     const int gz = (nslices + gy - 1) / gy;
     dim3 grid((unsigned)tiles, gy, gz);
     if (mode == 0) k_tiled<0, double><<<grid, kThreads, 0, st>>>(jd, s0, nslices, tn_bits);
+    else if (mode == 2) k_tiled<2, u64><<<grid, kThreads, 0, st>>>(jd, s0, nslices, tn_bits);
     else k_tiled<1, float><<<grid, kThreads, 0, st>>>(jd, s0, nslices, tn_bits);
   } else if (kernel == K_REDUCE) {
     const int64_t blocks = (int64_t)nslices << (jd.mb + jd.nb);
@@ -1738,9 +1827,11 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
     const bool vec = reduce_vec_ok(jd.a, mode) && reduce_vec_ok(jd.b, mode) && jd.kb >= 10;
     if (vec) {
       if (mode == 0) k_reduce_vec<0, double><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
+      else if (mode == 2) k_reduce_vec<2, u64><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
       else k_reduce_vec<1, float><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
     } else {
       if (mode == 0) k_reduce<0, double><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
+      else if (mode == 2) k_reduce<2, u64><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
       else k_reduce<1, float><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
     }
   } else if (launch_stream(mode, jd, s0, nslices, st)) {
@@ -1755,9 +1846,11 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
 #define TOGB_DIRECT(KK)                                                                          \
     if (vec == 4) {                                                                              \
       if (mode == 0) k_direct<0, double, KK, 4><<<g, kThreads, 0, st>>>(jd, s0, nslices);       \
+      else if (mode == 2) k_direct<2, u64, KK, 4><<<g, kThreads, 0, st>>>(jd, s0, nslices);     \
       else k_direct<1, float, KK, 4><<<g, kThreads, 0, st>>>(jd, s0, nslices);                  \
     } else {                                                                                     \
       if (mode == 0) k_direct<0, double, KK, 1><<<g, kThreads, 0, st>>>(jd, s0, nslices);       \
+      else if (mode == 2) k_direct<2, u64, KK, 1><<<g, kThreads, 0, st>>>(jd, s0, nslices);     \
       else k_direct<1, float, KK, 1><<<g, kThreads, 0, st>>>(jd, s0, nslices);                  \
     }
     switch (jd.kb) {
@@ -1777,12 +1870,14 @@ cudaError_t launch_once_list(int mode, const OnceList& ol, cudaStream_t st) {
   if (ol.n <= 0 || ol.total_tiles <= 0) return cudaSuccess;
   const int sms = sm_count();
   int per_sm = 0;
-  cudaError_t e = mode == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<0, double>, kThreads, 0)
-                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<1, float>, kThreads, 0);
+  cudaError_t e = mode == 0   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<0, double>, kThreads, 0)
+                  : mode == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<2, u64>, kThreads, 0)
+                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<1, float>, kThreads, 0);
   if (e != cudaSuccess || per_sm < 1) per_sm = 1;
   const int64_t wave = (int64_t)sms * per_sm;
   const int grid = (int)(ol.total_tiles < wave ? ol.total_tiles : wave);
   if (mode == 0) k_once_list<0, double><<<grid, kThreads, 0, st>>>(ol);
+  else if (mode == 2) k_once_list<2, u64><<<grid, kThreads, 0, st>>>(ol);
   else k_once_list<1, float><<<grid, kThreads, 0, st>>>(ol);
   return cudaGetLastError();
 }
@@ -1795,11 +1890,13 @@ cudaError_t launch_root(int mode, const RootDesc& rd, const int64_t* s0, int nsl
   }
   if (E <= 1024) {  // few root entries: a CTA per entry, slices across its threads
     if (mode == 0) k_root_tree<0, double><<<(unsigned)E, kThreads, 0, st>>>(rd, s0, nslices);
+    else if (mode == 2) k_root_tree<2, u64><<<(unsigned)E, kThreads, 0, st>>>(rd, s0, nslices);
     else k_root_tree<1, float><<<(unsigned)E, kThreads, 0, st>>>(rd, s0, nslices);
     return cudaGetLastError();
   }
   const int g = grid_for(E);
   if (mode == 0) k_root<0, double><<<g, kThreads, 0, st>>>(rd, s0, nslices);
+  else if (mode == 2) k_root<2, u64><<<g, kThreads, 0, st>>>(rd, s0, nslices);
   else k_root<1, float><<<g, kThreads, 0, st>>>(rd, s0, nslices);
   return cudaGetLastError();
 }
@@ -1813,6 +1910,12 @@ cudaError_t launch_build_leaves(const LeafBuild* items, int n, double* v64, floa
 
 cudaError_t launch_set_s0(int64_t* d_s0, int64_t value, cudaStream_t st) {
   k_set_s0<<<1, 1, 0, st>>>(d_s0, value);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_leaf_int(const double* v64, void* out, int64_t n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_leaf_int<<<grid_for(n), kThreads, 0, st>>>(v64, (u64*)out, n);
   return cudaGetLastError();
 }
 

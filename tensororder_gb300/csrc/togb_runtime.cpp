@@ -63,7 +63,7 @@ struct Node {
   std::vector<int> m_lsb, n_lsb, k_lsb;     // GEMM bit order, least significant first
   int64_t off = -1;              // arena offset (elements), joins only
   int kernel = togb::K_DIRECT;
-  int kernel_set[2] = {-1, -1}; // per-form kernel chosen by the caller (togb_program_set_kernel), -1 = default
+  int kernel_set[3] = {-1, -1, -1}; // per-form kernel chosen by the caller (togb_program_set_kernel), -1 = default
   bool dep = true;               // depends on the slice (reads a sliced leaf, directly or below)
   int slot = -1;                 // joins: index among the joins of its phase (metadata row)
 };
@@ -154,6 +154,11 @@ struct togb_program {
   double* d_leaf64 = nullptr;
   float* d_leaf32 = nullptr;    // split mode: FP32 rounding of each leaf value
   float* d_leaf32lo = nullptr;  // split mode: value - hi, rounded to FP32
+  int64_t num_leaf_values = 0;  // entries of every leaf array
+  // Int form: the FP64 leaf values converted toward zero, made from d_leaf64
+  // by the first int-form run after the leaves were created or replaced.
+  void* d_leaf_int = nullptr;
+  bool leaf_int_current = false;
   // planning
   int64_t arena = 0;       // per-slice elements (slice-dependent joins)
   int64_t arena_once = 0;  // elements of the slice-invariant joins, shared by all slices
@@ -161,7 +166,8 @@ struct togb_program {
   double flops_once = 0, bytes64_once = 0;  // once per run, slice-invariant joins
   int max_rank = 0;
   // device state
-  double* d_acc = nullptr;  // [2 * 2^root_rank]: sum then compensation
+  double* d_acc = nullptr;  // [2 * 2^root_rank]: sum then compensation (int form: wrapping words, then zeros)
+  int acc_kind = 0;         // what the accumulator holds since the last reset: 0 nothing, 1 FP64 sums, 2 int words
   int64_t* d_s0 = nullptr;
   int32_t* d_err = nullptr; // set by a kernel whose bounded wait expired
   int64_t wait_cycles = togb::kDefaultWaitCycles;  // limit of every device-side pipeline wait
@@ -208,7 +214,9 @@ struct togb_program {
 
 namespace {
 
-size_t elem_size(int mode) { return mode == TOGB_MODE_F64 ? 8 : 4; }
+size_t elem_size(int mode) { return mode == TOGB_MODE_SPLIT ? 4 : 8; }
+
+bool known_mode(int mode) { return mode == TOGB_MODE_F64 || mode == TOGB_MODE_SPLIT || mode == TOGB_MODE_INT64; }
 
 int64_t round256(int64_t x) { return (x + 255) / 256 * 256; }
 
@@ -453,7 +461,9 @@ void fill_operand(const togb_program* p, const Node& X, const std::vector<int>& 
   const size_t es = elem_size(mode);
   const WsLayout w = ws_layout(p, mode, ws, B);
   if (X.leaf >= 0) {
-    const char* base = mode == TOGB_MODE_F64 ? (const char*)p->d_leaf64 : (const char*)p->d_leaf32;
+    const char* base = mode == TOGB_MODE_F64     ? (const char*)p->d_leaf64
+                       : mode == TOGB_MODE_INT64 ? (const char*)p->d_leaf_int
+                                                 : (const char*)p->d_leaf32;
     od.ptr = base + p->leaf_off[X.leaf] * es;
     od.batch_stride = 0;
     const std::vector<int>& axes = p->leaf_axes[X.leaf];
@@ -518,9 +528,8 @@ int default_split_kernel(const togb_program* p, const Node& J) {
 
 // Kernel of a join in a form: the caller's choice if set, else the default.
 int join_kernel(const togb_program* p, const Node& J, int mode) {
-  const int m = mode == TOGB_MODE_SPLIT ? 1 : 0;
-  if (J.kernel_set[m] >= 0) return J.kernel_set[m];
-  return m ? default_split_kernel(p, J) : J.kernel;
+  if (known_mode(mode) && J.kernel_set[mode] >= 0) return J.kernel_set[mode];
+  return mode == TOGB_MODE_SPLIT ? default_split_kernel(p, J) : J.kernel;
 }
 
 int split_kernel(const togb_program* p, const Node& J) { return join_kernel(p, J, TOGB_MODE_SPLIT); }
@@ -534,7 +543,7 @@ bool kernel_allowed(const togb_program* p, const Node& J, int mode, int kernel) 
   switch (kernel) {
     case togb::K_DIRECT: return true;
     case togb::K_REDUCE: return mb + nb <= 20;  // one CTA per output entry and slice
-    case togb::K_TILED: return mode == TOGB_MODE_F64 || !leaf;
+    case togb::K_TILED: return mode != TOGB_MODE_SPLIT || !leaf;
     case togb::K_UMMA: return mode == TOGB_MODE_SPLIT && !leaf && mb >= 5 && nb >= 5 && kb >= 2;
     default: return false;
   }
@@ -1144,6 +1153,7 @@ togb_status lower_host(const togb_program_desc* d, int device, togb_program** ou
   for (const Node& n : p->nodes) p->max_rank = std::max(p->max_rank, n.rank);
   plan_layouts(p);
   plan_arena(p);
+  p->num_leaf_values = voff;
   *num_values = voff;
   *out = p;
   return TOGB_OK;
@@ -1336,6 +1346,7 @@ togb_status togb_program_set_leaves(togb_program* p, const togb_leaf_spec* specs
         togb::launch_build_leaves(p->d_items, (int)p->h_items.size(), p->d_leaf64, p->d_leaf32, p->d_leaf32lo, st);
     if (e != cudaSuccess) return cuda_fail(e, "leaf build");
   }
+  p->leaf_int_current = false;  // the int form converts the new values at its next run
   if (shift != p->leaf_shift) {  // the normalisers are part of the descriptors: rebuild them
     p->leaf_shift = shift;
     clear_graphs(p);
@@ -1357,7 +1368,7 @@ togb_status togb_program_create_host(const togb_program_desc* d, togb_program** 
 
 togb_status togb_program_describe(togb_program* p, int mode, int32_t join, char* buf, size_t n) {
   if (!p || !buf || n == 0) return fail(TOGB_ERR_INVALID, "null argument");
-  if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
+  if (!known_mode(mode)) return fail(TOGB_ERR_INVALID, "unknown mode");
   if (join < 0 || join >= (int32_t)p->joins.size()) return fail(TOGB_ERR_INVALID, "join index out of range");
   if (p->cur_mode != mode) {
     if (!p->host_only) return fail(TOGB_ERR_UNSUPPORTED, "describe a device program after a run in this mode");
@@ -1410,7 +1421,7 @@ togb_status togb_program_info_get(const togb_program* p, togb_program_info* info
   info->num_launches = (int32_t)p->per.size() + 1;
   info->flops_per_slice = p->flops;
   info->bytes_per_slice_f64 = p->bytes64;
-  for (int m = 0; m < 2; ++m) {
+  for (int m = 0; m < 3; ++m) {
     info->workspace_per_slice[m] = ws_per_slice(p, m);
     info->workspace_fixed[m] = ws_fixed(p, m);
   }
@@ -1426,11 +1437,13 @@ togb_status togb_program_reset(togb_program* p, void* stream) {
   TOGB_CUDA(cudaSetDevice(p->device));
   const int64_t E = pow2(p->nodes[p->root].rank);
   TOGB_CUDA(cudaMemsetAsync(p->d_acc, 0, 2 * E * 8, (cudaStream_t)stream));
+  p->acc_kind = 0;
   return TOGB_OK;
 }
 
 togb_status togb_program_joins(const togb_program* p, int mode, int32_t* out, int32_t n) {
   if (!p || !out) return fail(TOGB_ERR_INVALID, "null argument");
+  if (!known_mode(mode)) return fail(TOGB_ERR_INVALID, "unknown mode");
   if (n != (int32_t)p->joins.size()) return fail(TOGB_ERR_INVALID, "n must equal the number of joins");
   for (size_t j = 0; j < p->joins.size(); ++j) {
     const Node& J = p->nodes[p->joins[j]];
@@ -1445,7 +1458,7 @@ togb_status togb_program_joins(const togb_program* p, int mode, int32_t* out, in
 
 togb_status togb_program_launch_count(const togb_program* p, int mode, int64_t* launches) {
   if (!p || !launches) return fail(TOGB_ERR_INVALID, "null argument");
-  if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
+  if (!known_mode(mode)) return fail(TOGB_ERR_INVALID, "unknown mode");
   int64_t once = (int64_t)p->once.size();
   if (p->once_segs_mode == mode) {
     if (!p->once_segs.empty()) once = (int64_t)p->once_segs.size();
@@ -1461,14 +1474,13 @@ togb_status togb_program_launch_count(const togb_program* p, int mode, int64_t* 
 
 togb_status togb_program_set_kernel(togb_program* p, int mode, int32_t join, int32_t kernel) {
   if (!p) return fail(TOGB_ERR_INVALID, "null program");
-  if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
+  if (!known_mode(mode)) return fail(TOGB_ERR_INVALID, "unknown mode");
   if (join < 0 || join >= (int32_t)p->joins.size()) return fail(TOGB_ERR_INVALID, "join index out of range");
   Node& J = p->nodes[p->joins[join]];
   if (kernel >= 0 && !kernel_allowed(p, J, mode, kernel))
     return fail(TOGB_ERR_UNSUPPORTED, "kernel " + std::to_string(kernel) + " cannot run join " + std::to_string(join));
-  const int m = mode == TOGB_MODE_SPLIT ? 1 : 0;
-  if (J.kernel_set[m] != kernel) {
-    J.kernel_set[m] = kernel < 0 ? -1 : kernel;
+  if (J.kernel_set[mode] != kernel) {
+    J.kernel_set[mode] = kernel < 0 ? -1 : kernel;
     if (p->cur_mode == mode) {  // descriptors (TMA maps, operand order) follow the kernel choice
       clear_graphs(p);
       p->cur_mode = -1;
@@ -1480,6 +1492,7 @@ togb_status togb_program_set_kernel(togb_program* p, int mode, int32_t join, int
 togb_status togb_program_kernel_allowed(const togb_program* p, int mode, int32_t join, int32_t kernel,
                                         int32_t* allowed) {
   if (!p || !allowed) return fail(TOGB_ERR_INVALID, "null argument");
+  if (!known_mode(mode)) return fail(TOGB_ERR_INVALID, "unknown mode");
   if (join < 0 || join >= (int32_t)p->joins.size()) return fail(TOGB_ERR_INVALID, "join index out of range");
   *allowed = kernel_allowed(p, p->nodes[p->joins[join]], mode, kernel) ? 1 : 0;
   return TOGB_OK;
@@ -1515,11 +1528,28 @@ togb_status togb_program_run(togb_program* p, int mode, int64_t begin, int64_t e
                              size_t ws_bytes, void* stream_v) {
   if (!p) return fail(TOGB_ERR_INVALID, "null program");
   if (p->host_only) return fail(TOGB_ERR_UNSUPPORTED, "host-only program: create it with togb_program_create to run it");
-  if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
+  if (!known_mode(mode)) return fail(TOGB_ERR_INVALID, "unknown mode");
   if (begin < 0 || end > p->num_slices || begin > end) return fail(TOGB_ERR_INVALID, "slice range out of bounds");
+  const int kind = mode == TOGB_MODE_INT64 ? 2 : 1;
+  if (p->acc_kind != 0 && p->acc_kind != kind)
+    return fail(TOGB_ERR_INVALID, kind == 2 ? "the accumulator holds FP64 sums: reset it before an int-form run"
+                                            : "the accumulator holds int-form words: reset it before an FP64 or split run");
   if (begin == end) return TOGB_OK;
   cudaStream_t st = (cudaStream_t)stream_v;
   TOGB_CUDA(cudaSetDevice(p->device));
+  if (mode == TOGB_MODE_INT64 && !p->leaf_int_current) {
+    if (!p->d_leaf_int) {  // allocated once: descriptors keep its address
+      cudaError_t e = cudaMalloc(&p->d_leaf_int, std::max<int64_t>(p->num_leaf_values, 1) * 8);
+      if (e != cudaSuccess) {
+        p->d_leaf_int = nullptr;
+        return cuda_fail(e, "int-form leaf allocation");
+      }
+    }
+    cudaError_t e = togb::launch_leaf_int(p->d_leaf64, p->d_leaf_int, p->num_leaf_values, st);
+    if (e != cudaSuccess) return cuda_fail(e, "int-form leaf conversion");
+    p->leaf_int_current = true;
+  }
+  p->acc_kind = kind;
   const int64_t per = ws_per_slice(p, mode);
   const int64_t fixed = ws_fixed(p, mode);
   const int64_t want = end - begin;
@@ -1568,11 +1598,18 @@ togb_status togb_program_run(togb_program* p, int mode, int64_t begin, int64_t e
   return r;
 }
 
-togb_status togb_program_result(togb_program* p, void* stream, double* out, double* comp, int64_t n) {
+namespace {
+
+// Checks shared by the result entry points, then a wait for `stream` and the
+// device error word.
+togb_status result_ready(togb_program* p, void* stream, const void* out, int64_t n, int kind) {
   if (!p || !out) return fail(TOGB_ERR_INVALID, "null argument");
   if (p->host_only) return fail(TOGB_ERR_UNSUPPORTED, "host-only program has no result");
   const int64_t E = pow2(p->nodes[p->root].rank);
   if (n != E) return fail(TOGB_ERR_INVALID, "result size does not match the root tensor");
+  if (p->acc_kind != 0 && p->acc_kind != kind)
+    return fail(TOGB_ERR_INVALID, kind == 2 ? "the accumulator holds FP64 sums: read it with togb_program_result"
+                                            : "the accumulator holds int-form words: read it with togb_program_result_u64");
   TOGB_CUDA(cudaSetDevice(p->device));
   TOGB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
   int32_t err = 0;
@@ -1583,6 +1620,22 @@ togb_status togb_program_result(togb_program* p, void* stream, double* out, doub
                 "a device-side wait ran out of its limit (a fused slice-invariant list waiting for a producer "
                 "tile, or a tensor-core join waiting in its load/MMA/read-out pipeline); the result is invalid");
   }
+  return TOGB_OK;
+}
+
+}  // namespace
+
+togb_status togb_program_result_u64(togb_program* p, void* stream, uint64_t* out, int64_t n) {
+  togb_status r = result_ready(p, stream, out, n, 2);
+  if (r != TOGB_OK) return r;
+  TOGB_CUDA(cudaMemcpy(out, p->d_acc, n * 8, cudaMemcpyDeviceToHost));
+  return TOGB_OK;
+}
+
+togb_status togb_program_result(togb_program* p, void* stream, double* out, double* comp, int64_t n) {
+  togb_status r = result_ready(p, stream, out, n, 1);
+  if (r != TOGB_OK) return r;
+  const int64_t E = n;
   std::vector<double> h(2 * E);
   TOGB_CUDA(cudaMemcpy(h.data(), p->d_acc, 2 * E * 8, cudaMemcpyDeviceToHost));
   for (int64_t i = 0; i < E; ++i) {
@@ -1603,6 +1656,7 @@ void togb_program_destroy(togb_program* p) {
   cudaFree(p->d_leaf64);
   cudaFree(p->d_leaf32);
   cudaFree(p->d_leaf32lo);
+  cudaFree(p->d_leaf_int);
   cudaFree(p->d_acc);
   cudaFree(p->d_s0);
   cudaFree(p->d_err);
@@ -1647,6 +1701,7 @@ void batch_free(togb_batch* b) {
 togb_status enqueue_count(togb_program* p, int mode, int64_t B, cudaStream_t st) {
   const int64_t E = pow2(p->nodes[p->root].rank);
   TOGB_CUDA(cudaMemsetAsync(p->d_acc, 0, 2 * E * 8, st));
+  p->acc_kind = 1;  // batches run the FP64 and split forms
   togb_status r = enqueue_phase(p, mode, true, 1, st, nullptr);
   for (int64_t s = 0; r == TOGB_OK && s < p->num_slices; s += B) {
     const int nb = (int)std::min<int64_t>(B, p->num_slices - s);
@@ -1665,7 +1720,8 @@ togb_status togb_batch_create(togb_program* const* progs, int32_t n, int mode, v
                               const size_t* ws_bytes, int32_t nstreams, togb_batch** out) {
   if (!progs || !workspaces || !ws_bytes || !out || n <= 0 || nstreams <= 0 || nstreams > 64)
     return fail(TOGB_ERR_INVALID, "bad batch arguments");
-  if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT) return fail(TOGB_ERR_INVALID, "unknown mode");
+  if (mode != TOGB_MODE_F64 && mode != TOGB_MODE_SPLIT)
+    return fail(TOGB_ERR_INVALID, "batches run the FP64 and split forms");
   *out = nullptr;
   togb_batch* b = new togb_batch();
   b->mode = mode;

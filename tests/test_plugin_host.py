@@ -22,8 +22,15 @@ def test_entry_types_and_sizes():
     s = api.GB300SplitAPI()
     s.add_argument("entry_type", "float64")
     assert s.get_entry_size() == 4
+    h = api.GB300API()
+    h.add_argument("entry_type", "float16")  # FP32 storage: at least float16
+    assert h._mode == runtime.MODE_SPLIT and h.get_entry_size() == 4
+    for name, word in (("int", np.int64), ("uint", np.uint64)):
+        q = api.GB300SplitAPI()
+        q.add_argument("entry_type", name)
+        assert q._mode == runtime.MODE_INT64 and q._word_type is word and q.get_entry_size() == 8
     with pytest.raises(ValueError):
-        p.add_argument("entry_type", "float16")
+        p.add_argument("entry_type", "bigint")  # no device form, as in the reference's GPU backend
     with pytest.raises(ValueError):
         p.add_argument("tpu", "1.2.3.4")
     p.add_argument("thread_limit", 1)
