@@ -16,8 +16,10 @@ from oracle import refload
 pytestmark = pytest.mark.skipif(not refload.available(), reason="reference checkout / oracle build absent")
 
 
-@pytest.mark.parametrize("library,mode", [("gb300", 0), ("gb300-split", 1)])
-def test_cli_selects_plugin(library, mode, monkeypatch, capsys):
+@pytest.mark.parametrize("library,entry,mode", [("gb300", "float64", 0), ("gb300-split", "float64", 1),
+                                                ("gb300", "float32", 1), ("gb300", "int", 2),
+                                                ("gb300-split", "uint", 2)])
+def test_cli_selects_plugin(library, entry, mode, monkeypatch, capsys):
     refload.load()
     from oracle import contract
     from tensororder_gb300 import api, launcher
@@ -26,7 +28,8 @@ def test_cli_selects_plugin(library, mode, monkeypatch, capsys):
 
     def stub(self, prog, limit):
         calls.append((prog.num_joins, prog.num_slices, self._mode))
-        return np.asarray(contract.contract_sliced(prog, limit))
+        dtype = self._word_type if self._mode == 2 else np.float64
+        return np.asarray(contract.contract_sliced(prog, limit, dtype=dtype))
 
     monkeypatch.setattr(api.GB300API, "_run", stub)
     monkeypatch.setattr(api, "_OOM", api._OOM)  # register() rebinds it; restore afterwards
@@ -36,7 +39,7 @@ def test_cli_selects_plugin(library, mode, monkeypatch, capsys):
     with pytest.raises(SystemExit) as exc:
         launcher.main(["--reference-src", refload.reference_src(), "tensororder", "--planner", "line-Flow",
                        "--weights", "unweighted", "--tensor_library", library, "--timeout", "3",
-                       "--minimum_slice", "2"])
+                       "--minimum_slice", "2", "--entry_type", entry])
     assert exc.value.code == 0
     out = capsys.readouterr().out
     assert "Count: 2802717837" in out
