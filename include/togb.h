@@ -45,12 +45,17 @@ typedef enum {
   TOGB_MODE_F64 = 0,   /* plain form: FP64 storage and arithmetic          */
   TOGB_MODE_SPLIT = 1, /* chosen form: FP32 storage with a per-slice power-of-two
                           exponent per tensor; FP64 only in the slice sum  */
-  TOGB_MODE_INT64 = 2  /* int form: 64-bit integer storage and arithmetic
+  TOGB_MODE_INT64 = 2, /* int form: 64-bit integer storage and arithmetic
                           modulo 2^64, the reference's "int" and "uint"
                           entry types (numpy int64 / uint64,
                           src/tensor_network/tensor_apis/numpy_apis.py:15-22).
                           Leaf values are converted toward zero.  Read the
                           result with togb_program_result_u64.        */
+  TOGB_MODE_MOD = 3    /* residue form: the int form's integers modulo the
+                          program's modulus (togb_program_set_modulus, below
+                          2^28), for exact counts by the Chinese remainder
+                          theorem (the reference's "bigint" entry type).
+                          Read the result with togb_program_result_u64. */
 } togb_mode;
 
 typedef struct togb_program togb_program;
@@ -85,8 +90,8 @@ typedef struct {
   int32_t num_launches;          /* kernel launches per chunk of slices        */
   double flops_per_slice;        /* per-slice joins: sum of 2*M*N*K            */
   double bytes_per_slice_f64;    /* per-slice joins: sum of 8*(M*K + K*N + M*N) */
-  int64_t workspace_per_slice[3];/* workspace bytes per slice, by togb_mode    */
-  int64_t workspace_fixed[3];    /* workspace bytes independent of slice count */
+  int64_t workspace_per_slice[4];/* workspace bytes per slice, by togb_mode    */
+  int64_t workspace_fixed[4];    /* workspace bytes independent of slice count */
   int32_t num_joins_once;        /* slice-invariant joins                      */
   int32_t pad_;
   double flops_once;             /* slice-invariant joins: sum of 2*M*N*K      */
@@ -154,9 +159,9 @@ togb_status togb_program_create_host(const togb_program_desc* desc, togb_program
 togb_status togb_program_describe(togb_program* prog, int mode, int32_t join, char* buf, size_t n);
 
 /* Zero the device-side slice accumulator (compensated FP64 sum, or the int
- * form's words).  Runs between two resets must use forms of one kind: FP64
- * and split runs add FP64 sums, int-form runs add 64-bit words
- * (TOGB_ERR_INVALID otherwise). */
+ * forms' words).  Runs between two resets must use forms of one kind: FP64
+ * and split runs add FP64 sums, int-form runs add 64-bit words, residue-form
+ * runs add residues of one modulus (TOGB_ERR_INVALID otherwise). */
 togb_status togb_program_reset(togb_program* prog, void* stream);
 
 /* Contract slices [slice_begin, slice_end) in `mode` and add them into the
@@ -172,11 +177,16 @@ togb_status togb_program_run(togb_program* prog, int mode, int64_t slice_begin, 
  * together with the compensation terms (`comp`, may be NULL). */
 togb_status togb_program_result(togb_program* prog, void* stream, double* out, double* comp, int64_t n);
 
-/* The int form's result: wait for `stream` and copy the accumulated root
- * tensor (2^root_rank 64-bit words, the sums modulo 2^64; read them as int64
- * or uint64) to host `out`.  TOGB_ERR_INVALID when the accumulator holds FP64
- * sums. */
+/* The int forms' result: wait for `stream` and copy the accumulated root
+ * tensor (2^root_rank 64-bit words: the sums modulo 2^64, to be read as int64
+ * or uint64, or their residues modulo the program's modulus) to host `out`.
+ * TOGB_ERR_INVALID when the accumulator holds FP64 sums. */
 togb_status togb_program_result_u64(togb_program* prog, void* stream, uint64_t* out, int64_t n);
+
+/* The residue form's modulus, in [2, 2^28).  Runs in TOGB_MODE_MOD compute
+ * modulo it; changing it rebuilds that form's descriptors at its next run.
+ * Between two resets every residue-form run must use the same modulus. */
+togb_status togb_program_set_modulus(togb_program* prog, uint64_t modulus);
 
 /* Per join in post-order, five int32: log2 M, log2 N, log2 K over unsliced
  * axes, the kernel used in `mode` (0 thread-per-output, 1 tiled SIMT GEMM,

@@ -16,8 +16,11 @@ library's form, ``float32`` and ``float16`` take the split form (FP32 storage,
 at least float16's range and precision), ``int`` and ``uint`` take the int
 form (64-bit words, sums and products modulo 2^64, as numpy's int64 and
 uint64 tensors wrap; the count is a numpy int64 or uint64 scalar).
-``bigint`` (numpy object arrays) has no device form and is refused, as the
-reference's GPU backend refuses it.
+``bigint`` (numpy object arrays of Python integers) gives the exact count as a
+Python int, recovered from the int form's count modulo 2^64 and residue-form
+counts modulo primes below 2^28 (:mod:`tensororder_gb300.exact`); networks
+with non-integer leaf values give the plain FP64 count as a Python float, as
+the reference's object arithmetic turns floating there.
 
 ``contract_sliced`` is the hot path.  It flattens the plan
 (:func:`tensororder_gb300.program.from_plan`), hands it to libtogb and runs the
@@ -37,6 +40,7 @@ import time
 
 import numpy as np
 
+from . import exact
 from . import program as _program
 from . import runtime
 
@@ -56,7 +60,8 @@ class GB300API:
     slices_per_call = 1 << 14  # upper bound on slices queued by one C call
     max_call_seconds = 0.25    # target device time of one call (timeout granularity)
     # device rate for sizing the first call before any has been timed (FLOP/s)
-    _first_call_rate = {runtime.MODE_F64: 1.0e12, runtime.MODE_SPLIT: 5.0e13, runtime.MODE_INT64: 3.0e11}
+    _first_call_rate = {runtime.MODE_F64: 1.0e12, runtime.MODE_SPLIT: 5.0e13, runtime.MODE_INT64: 3.0e11,
+                        runtime.MODE_MOD: 1.5e11}
     # numpy type of the int form's count, by entry type
     _word_types = {"int": np.int64, "uint": np.uint64}
 
@@ -67,6 +72,7 @@ class GB300API:
     def __init__(self, mode=runtime.MODE_F64, device=0):
         self._mode = mode
         self._word_type = np.int64  # the int form's count type
+        self._bigint = False        # exact counts through the int forms
         self._device = device
         self._thread_limit = None
         self.last_program = None
@@ -75,16 +81,15 @@ class GB300API:
     # -- configuration (numpy_apis.py:13-34) --------------------------------
     def add_argument(self, key, value):
         if key == "entry_type":
-            if value == "float64":
-                return
+            if value not in ("float64", "float32", "float16", "bigint") and value not in self._word_types:
+                raise ValueError("Unknown gb300 type %s" % value)
+            self._bigint = value == "bigint"
             if value in ("float32", "float16"):
                 self._mode = runtime.MODE_SPLIT
-                return
-            if value in self._word_types:
+            elif value in self._word_types:
                 self._mode = runtime.MODE_INT64
                 self._word_type = self._word_types[value]
-                return
-            raise ValueError("Unknown gb300 type %s" % value)
+            return
         if key == "thread_limit":
             # Host thread cap of the numpy backend; the device path has no host
             # compute threads to limit.
@@ -93,7 +98,7 @@ class GB300API:
         raise ValueError("Invalid argument " + str(key) + " for selected tensor_library")
 
     def get_entry_size(self):
-        return 4 if self._mode == runtime.MODE_SPLIT else 8
+        return 4 if self._mode == runtime.MODE_SPLIT and not self._bigint else 8
 
     # -- tensor primitives ---------------------------------------------------
     def create_tensor(self, shape, default_value=None):
@@ -200,25 +205,56 @@ class GB300API:
             stream = self._stream()
             dp = self._program(prog, stream)
             self.last_program = dp
-            dp.reset(stream)
-            ws = dp.allocate_workspace(self._mode, max(n, 1))
-            # First call sized from the FLOP count, later ones from the measured
-            # time per slice of the previous call.
-            per_slice = max(float(dp.info.flops_per_slice), 1.0) / self._first_call_rate[self._mode]
-            s = 0
-            while s < n:
-                k = int(min(self.slices_per_call, max(1, self.max_call_seconds / max(per_slice, 1e-9))))
-                e = min(n, s + k)
-                t0 = time.perf_counter()
-                dp.run(self._mode, s, e, workspace=ws, stream=stream)
-                self._wait(stream)
-                per_slice = (time.perf_counter() - t0) / (e - s)
-                s = e
+            if self._bigint:
+                return self._exact(prog, dp, n, stream)
+            self._count(dp, self._mode, n, stream)
             if self._mode == runtime.MODE_INT64:
                 return dp.result_words(stream, self._word_type)
             return dp.result(stream)
         except runtime.DeviceOutOfMemory as exc:
             raise _OOM(str(exc))
+
+    def _count(self, dp, mode, n, stream):
+        """Reset the accumulator and add slices [0, n) in ``mode``, as calls of
+        bounded device time with a wait after each."""
+        dp.reset(stream)
+        ws = dp.allocate_workspace(mode, max(n, 1))
+        # First call sized from the FLOP count, later ones from the measured
+        # time per slice of the previous call.
+        per_slice = max(float(dp.info.flops_per_slice), 1.0) / self._first_call_rate[mode]
+        s = 0
+        while s < n:
+            k = int(min(self.slices_per_call, max(1, self.max_call_seconds / max(per_slice, 1e-9))))
+            e = min(n, s + k)
+            t0 = time.perf_counter()
+            dp.run(mode, s, e, workspace=ws, stream=stream)
+            self._wait(stream)
+            per_slice = (time.perf_counter() - t0) / (e - s)
+            s = e
+
+    def _exact(self, prog, dp, n, stream):
+        """The ``bigint`` count: exact Python integers from the int forms'
+        residues, or the plain FP64 count (Python floats) when a leaf value is
+        not an integer."""
+        if not exact.integer_leaves(prog):
+            self._count(dp, runtime.MODE_F64, n, stream)
+            return dp.result(stream).astype(object)
+        # Leaf values are non-negative (program creation refuses others), so
+        # the split form's count bounds the count to about 1e-6.
+        self._count(dp, runtime.MODE_SPLIT, n, stream)
+        bound = float(np.max(np.abs(dp.result(stream))))
+        moduli = exact.moduli_for(bound * (1.0 + 1e-4) + 1.0)
+        self._count(dp, runtime.MODE_INT64, n, stream)
+        words = dp.result_words(stream, np.uint64)
+        residues = []
+        for p in moduli:
+            dp.set_modulus(p)
+            self._count(dp, runtime.MODE_MOD, n, stream)
+            residues.append(dp.result_words(stream, np.uint64).reshape(-1))
+        out = np.empty(words.size, dtype=object)
+        for i, w in enumerate(words.reshape(-1)):
+            out[i] = exact.combine(int(w), [int(r[i]) for r in residues], moduli)
+        return out.reshape(words.shape)
 
 
 class GB300SplitAPI(GB300API):

@@ -79,6 +79,9 @@ struct JoinDesc {
   int64_t dot_y_bs;    // elements of Y between slices (0 when Y is shared by every slice)
   double* dot_part;    // slice b's partials at dot_part + b * dot_part_bs, tile t's warp w at t * 8 + w
   int64_t dot_part_bs;
+  // Residue form: words are residues modulo mod_p (below 2^28);
+  // mod_m = floor((2^64 - 1) / mod_p) for Barrett reduction.  Zero otherwise.
+  uint64_t mod_p, mod_m;
 };
 
 // Root reduction: adds every slice's root tensor into the compensated FP64
@@ -100,6 +103,7 @@ struct RootDesc {
   const int32_t* py_exp;
   int32_t npart;
   int32_t py_step;
+  uint64_t mod_p, mod_m;  // residue form: the modulus and its Barrett constant
 };
 
 namespace togb {
@@ -140,6 +144,7 @@ struct OnceJoin {
   int32_t mb, nb, kb, natural;
   int32_t a_ktab[16], b_ktab[16];
   Runs a_outer, b_outer, a_k, b_k, inv_m, inv_n;
+  uint64_t mod_p, mod_m;     // residue form: the modulus and its Barrett constant
 };
 struct OnceList {
   const OnceJoin* joins;     // device [n]
@@ -192,6 +197,8 @@ cudaError_t launch_build_leaves(const LeafBuild* items, int n, double* v64, floa
                                 cudaStream_t st);
 // The int form's leaf words: out[i] = the int64 value of v64[i] rounded toward zero.
 cudaError_t launch_leaf_int(const double* v64, void* out, int64_t n, cudaStream_t st);
+// The residue form's leaf words: that int64 value modulo p, in [0, p).
+cudaError_t launch_leaf_mod(const double* v64, void* out, int64_t n, uint64_t p, cudaStream_t st);
 // out[e] = acc[e] + acc[E + e]: the compensated sum of a root accumulator.
 cudaError_t launch_finalize(const double* acc, int64_t E, double* out, cudaStream_t st);
 cudaError_t probe_peak(int kind, cudaStream_t st, double* flops);

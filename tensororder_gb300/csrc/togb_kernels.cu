@@ -40,8 +40,9 @@ namespace {
 
 constexpr int kThreads = 256;
 
-// Element type of the int form: 64-bit words with wrapping (modulo 2^64)
-// arithmetic, which gives int64 and uint64 sums and products bit for bit.
+// Element type of the int forms: 64-bit words.  MODE 2 (int form) wraps
+// modulo 2^64, which gives int64 and uint64 sums and products bit for bit;
+// MODE 3 (residue form) keeps residues modulo a prime p < 2^28.
 using u64 = unsigned long long;
 
 // The FP64 form's multiply-add is an FMA; the int form's wraps.
@@ -49,22 +50,50 @@ __device__ __forceinline__ double mad(double a, double b, double c) { return fma
 __device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ u64 mad(u64 a, u64 b, u64 c) { return a * b + c; }
 
+// x mod p for x < 2^63 by Barrett reduction, m = floor((2^64 - 1) / p):
+// q = floor(x * m / 2^64) is floor(x / p) or one less (x * m / 2^64 falls short
+// of x / p by less than x / 2^64 + x / (p 2^64) < 1), so one conditional
+// subtraction finishes.
+__device__ __forceinline__ u64 mod_reduce(u64 x, u64 p, u64 m) {
+  const u64 r = x - __umul64hi(x, m) * p;
+  return r >= p ? r - p : r;
+}
+
+// The form's multiply-add and sum of two words.  Residues a, b, c < p < 2^28
+// give a * b + c < 2^57.  The modulus arguments are unused outside MODE 3.
+template <int MODE, class T>
+__device__ __forceinline__ T madm(T a, T b, T c, u64 p, u64 m) {
+  if constexpr (MODE == 3) return mod_reduce(a * b + c, p, m);
+  else return mad(a, b, c);
+}
+template <int MODE>
+__device__ __forceinline__ u64 addm(u64 a, u64 b, u64 p) {
+  if constexpr (MODE == 3) {
+    const u64 s = a + b;
+    return s >= p ? s - p : s;
+  } else {
+    return a + b;
+  }
+}
+
 // 16-byte vector of an element type.
 template <class T> struct Vec16;
 template <> struct Vec16<float> { using type = float4; };
 template <> struct Vec16<double> { using type = double2; };
 template <> struct Vec16<u64> { using type = ulonglong2; };
 
-// Wrapping sum of one word per thread over the CTA; the total in thread 0.
-// Every thread of the CTA must call it.
-__device__ __forceinline__ u64 block_sum_u64(u64 v) {
+// Sum of one word per thread over the CTA in the form's arithmetic (MODE 2
+// wrapping, MODE 3 modulo p); the total in thread 0.  Every thread of the CTA
+// must call it.
+template <int MODE>
+__device__ __forceinline__ u64 block_sum(u64 v, u64 p) {
   __shared__ u64 red[kThreads / 32];
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  for (int off = 16; off > 0; off >>= 1) v = addm<MODE>(v, __shfl_xor_sync(0xffffffffu, v, off), p);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
   u64 t = 0;
   if (threadIdx.x == 0)
-    for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+    for (int w = 0; w < kThreads / 32; ++w) t = addm<MODE>(t, red[w], p);
   return t;
 }
 
@@ -100,7 +129,7 @@ __device__ __forceinline__ T dot_k(const JoinDesc& jd, const T* __restrict__ A, 
     } else {
       T acc = 0;
 #pragma unroll
-      for (int k = 0; k < KK; ++k) acc = mad(av[k], bv[k], acc);
+      for (int k = 0; k < KK; ++k) acc = madm<MODE, T>(av[k], bv[k], acc, jd.mod_p, jd.mod_m);
       return acc;
     }
   } else {
@@ -130,7 +159,7 @@ __device__ __forceinline__ T dot_k(const JoinDesc& jd, const T* __restrict__ A, 
     } else {
       T acc = 0;
       for (int k = 0; k < K; ++k) {
-        acc = mad(A[oa + ka], B[ob + kb], acc);
+        acc = madm<MODE, T>(A[oa + ka], B[ob + kb], acc, jd.mod_p, jd.mod_m);
         const int t = __ffs(~k) - 1;
         ka += jd.a.dk[t];
         kb += jd.b.dk[t];
@@ -484,7 +513,7 @@ __global__ void __launch_bounds__(kThreads) k_direct_staged(const __grid_constan
         } else {
           T acc = 0;
 #pragma unroll
-          for (int k = 0; k < KK; ++k) acc = mad(ar[k], br[k], acc);
+          for (int k = 0; k < KK; ++k) acc = madm<MODE, T>(ar[k], br[k], acc, jd.mod_p, jd.mod_m);
           out[j] = acc;
         }
       }
@@ -781,7 +810,7 @@ __device__ __forceinline__ T once_dot(const OnceJoin& oj, int K, const T* av, co
     T acc = 0;
 #pragma unroll
     for (int k = 0; k < KMAX; ++k)
-      if (k < K) acc = mad(av[k], bv[k], acc);
+      if (k < K) acc = madm<MODE, T>(av[k], bv[k], acc, oj.mod_p, oj.mod_m);
     return acc;
   }
 }
@@ -804,7 +833,8 @@ __device__ T once_dot_serial(const OnceJoin& oj, int64_t oa, int64_t ob, int K, 
     return (T)f;
   } else {
     T acc = 0;
-    for (int k = 0; k < K; ++k) acc = mad(__ldcg(A + oa + oj.a_ktab[k]), __ldcg(B + ob + oj.b_ktab[k]), acc);
+    for (int k = 0; k < K; ++k)
+      acc = madm<MODE, T>(__ldcg(A + oa + oj.a_ktab[k]), __ldcg(B + ob + oj.b_ktab[k]), acc, oj.mod_p, oj.mod_m);
     return acc;
   }
 }
@@ -833,7 +863,8 @@ __device__ T once_dot_long(const OnceJoin& oj, int64_t oa, int64_t ob, int K, fl
   } else {
     T acc = 0;
     for (int k = 0; k < K; ++k)
-      acc = mad(__ldcg(A + oa + dep(oj.a_k, (uint64_t)k)), __ldcg(B + ob + dep(oj.b_k, (uint64_t)k)), acc);
+      acc = madm<MODE, T>(__ldcg(A + oa + dep(oj.a_k, (uint64_t)k)), __ldcg(B + ob + dep(oj.b_k, (uint64_t)k)), acc,
+                          oj.mod_p, oj.mod_m);
     return acc;
   }
 }
@@ -1083,6 +1114,14 @@ __global__ void __launch_bounds__(kThreads) k_tiled(const __grid_constant__ Join
 #pragma unroll
           for (int j = 0; j < 4; ++j) acc[i][j] = mad(av[i], bv[j], acc[i][j]);
       }
+      if constexpr (MODE == 3) {
+        // Residues below p < 2^28: a chunk adds BK = 16 products below 2^56
+        // to a residue, less than 2^61, so one reduction per chunk suffices.
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = mod_reduce(acc[i][j], jd.mod_p, jd.mod_m);
+      }
     } else {
       T part[4][4];
 #pragma unroll
@@ -1171,21 +1210,21 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const __grid_constant__ Joi
   int64_t pa8 = 0, pb8 = 0;
   for (int i = 0; i < LOGT && i < jd.kb; ++i) { pa8 += jd.a.s_k[i]; pb8 += jd.b.s_k[i]; }
   const int64_t steps = (jd.kb > LOGT) ? (1ll << (jd.kb - LOGT)) : (tid < (1 << jd.kb) ? 1 : 0);
-  if constexpr (MODE == 2) {  // int form: a wrapping sum, no compensation
+  if constexpr (MODE >= 2) {  // int forms: an exact sum in the form's arithmetic
     u64 sum = 0;
     constexpr int U = 4;
     for (int64_t j0 = 0; j0 < steps; j0 += U) {
       u64 y[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        y[u] = (j0 + u < steps) ? A[ka] * B[kb] : 0ull;
+        y[u] = (j0 + u < steps) ? madm<MODE, T>(A[ka], B[kb], 0ull, jd.mod_p, jd.mod_m) : 0ull;
         const int t8 = __ffsll(~(unsigned long long)(j0 + u)) - 1 + LOGT;
         if (t8 < TOGB_MAXBITS) { ka += jd.a.dk[t8] + pa8; kb += jd.b.dk[t8] + pb8; }
       }
 #pragma unroll
-      for (int u = 0; u < U; ++u) sum += y[u];
+      for (int u = 0; u < U; ++u) sum = addm<MODE>(sum, y[u], jd.mod_p);
     }
-    const u64 total = block_sum_u64(sum);
+    const u64 total = block_sum<MODE>(sum, jd.mod_p);
     if (tid == 0) ((T*)jd.c_ptr)[(int64_t)b * jd.c_batch_stride + dep(jd.r_cm, m) + dep(jd.r_cn, n)] = total;
     return;
   }
@@ -1316,18 +1355,18 @@ __global__ void __launch_bounds__(kThreads) k_reduce_vec(const __grid_constant__
       const T* x = reinterpret_cast<const T*>(&av[u]);
       const T* y = reinterpret_cast<const T*>(&bv[u]);
 #pragma unroll
-      for (int q = 0; q < VW; ++q) part = mad(x[q] * fa, y[q] * fb, part);
+      for (int q = 0; q < VW; ++q) part = madm<MODE, T>(x[q] * fa, y[q] * fb, part, jd.mod_p, jd.mod_m);
     }
-    if constexpr (MODE == 2) {
-      sum += part;
+    if constexpr (MODE >= 2) {
+      sum = addm<MODE>(sum, part, jd.mod_p);
     } else {
       const T t = sum + part;
       comp += fabs(sum) >= fabs(part) ? (sum - t) + part : (part - t) + sum;
       sum = t;
     }
   }
-  if constexpr (MODE == 2) {  // int form: a wrapping sum over the CTA
-    const u64 total = block_sum_u64(sum);
+  if constexpr (MODE >= 2) {  // int forms: an exact sum over the CTA
+    const u64 total = block_sum<MODE>(sum, jd.mod_p);
     if (tid == 0) ((T*)jd.c_ptr)[(int64_t)b * jd.c_batch_stride + dep(jd.r_cm, m) + dep(jd.r_cn, n)] = total;
     return;
   }
@@ -1358,12 +1397,12 @@ __global__ void k_root(const __grid_constant__ RootDesc rd, const int64_t* __res
   const int64_t E = 1ll << rd.r.outer_bits;
   const int64_t s0 = d_s0 ? *d_s0 : 0;
   const T* __restrict__ R = (const T*)rd.r.ptr;
-  if constexpr (MODE == 2) {  // int form: the accumulator's sums are wrapping words
+  if constexpr (MODE >= 2) {  // int forms: the accumulator's sums are words of the form
     u64* acc = reinterpret_cast<u64*>(rd.acc_sum);
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
       u64 sum = acc[e];
       const int64_t oe = dep(rd.r.r_outer, (uint64_t)e);
-      for (int b = 0; b < nslices; ++b) sum += R[slice_offset(rd.r, b, s0 + b) + oe];
+      for (int b = 0; b < nslices; ++b) sum = addm<MODE>(sum, R[slice_offset(rd.r, b, s0 + b) + oe], rd.mod_p);
       acc[e] = sum;
     }
   } else {
@@ -1408,11 +1447,15 @@ __global__ void __launch_bounds__(kThreads) k_root_tree(const __grid_constant__ 
   const int64_t s0 = d_s0 ? *d_s0 : 0;
   const T* __restrict__ R = (const T*)rd.r.ptr;
   const int64_t oe = dep(rd.r.r_outer, (uint64_t)e);
-  if constexpr (MODE == 2) {  // int form: a wrapping sum, added into the accumulator's word
+  if constexpr (MODE >= 2) {  // int forms: an exact sum, added into the accumulator's word
     u64 isum = 0;
-    for (int b = threadIdx.x; b < nslices; b += kThreads) isum += R[slice_offset(rd.r, b, s0 + b) + oe];
-    const u64 total = block_sum_u64(isum);
-    if (threadIdx.x == 0) reinterpret_cast<u64*>(rd.acc_sum)[e] += total;
+    for (int b = threadIdx.x; b < nslices; b += kThreads)
+      isum = addm<MODE>(isum, R[slice_offset(rd.r, b, s0 + b) + oe], rd.mod_p);
+    const u64 total = block_sum<MODE>(isum, rd.mod_p);
+    if (threadIdx.x == 0) {
+      u64* acc = reinterpret_cast<u64*>(rd.acc_sum) + e;
+      *acc = addm<MODE>(*acc, total, rd.mod_p);
+    }
     return;
   }
   double sum = 0.0, comp = 0.0;
@@ -1536,6 +1579,14 @@ __global__ void k_build_leaves(const LeafBuild* __restrict__ items, double* __re
 __global__ void k_leaf_int(const double* __restrict__ v64, u64* __restrict__ out, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     out[i] = (u64)__double2ll_rz(v64[i]);
+}
+
+// The residue form's leaves: the same integer value modulo p, in [0, p).
+__global__ void k_leaf_mod(const double* __restrict__ v64, u64* __restrict__ out, int64_t n, long long p) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const long long r = __double2ll_rz(v64[i]) % p;
+    out[i] = (u64)(r < 0 ? r + p : r);
+  }
 }
 
 __global__ void k_finalize(const double* __restrict__ acc, int64_t E, double* __restrict__ out) {
@@ -1668,6 +1719,7 @@ bool launch_staged(int mode, const JoinDesc& jd, const int64_t* s0, int nslices,
   {                                                                                                        \
     if (mode == 0) staged_launch(k_direct_staged<0, double, KK>, jd, si, s0, nslices, tiles, bytes, st);   \
     else if (mode == 2) staged_launch(k_direct_staged<2, u64, KK>, jd, si, s0, nslices, tiles, bytes, st); \
+    else if (mode == 3) staged_launch(k_direct_staged<3, u64, KK>, jd, si, s0, nslices, tiles, bytes, st); \
     else staged_launch(k_direct_staged<1, float, KK>, jd, si, s0, nslices, tiles, bytes, st);              \
   }
   switch (jd.kb) {
@@ -1818,6 +1870,7 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
     dim3 grid((unsigned)tiles, gy, gz);
     if (mode == 0) k_tiled<0, double><<<grid, kThreads, 0, st>>>(jd, s0, nslices, tn_bits);
     else if (mode == 2) k_tiled<2, u64><<<grid, kThreads, 0, st>>>(jd, s0, nslices, tn_bits);
+    else if (mode == 3) k_tiled<3, u64><<<grid, kThreads, 0, st>>>(jd, s0, nslices, tn_bits);
     else k_tiled<1, float><<<grid, kThreads, 0, st>>>(jd, s0, nslices, tn_bits);
   } else if (kernel == K_REDUCE) {
     const int64_t blocks = (int64_t)nslices << (jd.mb + jd.nb);
@@ -1828,10 +1881,12 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
     if (vec) {
       if (mode == 0) k_reduce_vec<0, double><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
       else if (mode == 2) k_reduce_vec<2, u64><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
+      else if (mode == 3) k_reduce_vec<3, u64><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
       else k_reduce_vec<1, float><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
     } else {
       if (mode == 0) k_reduce<0, double><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
       else if (mode == 2) k_reduce<2, u64><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
+      else if (mode == 3) k_reduce<3, u64><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
       else k_reduce<1, float><<<dim3(gx, gy), kThreads, 0, st>>>(jd, s0, nslices);
     }
   } else if (launch_stream(mode, jd, s0, nslices, st)) {
@@ -1847,10 +1902,12 @@ cudaError_t launch_join(int mode, int kernel, const JoinDesc& jd, const int64_t*
     if (vec == 4) {                                                                              \
       if (mode == 0) k_direct<0, double, KK, 4><<<g, kThreads, 0, st>>>(jd, s0, nslices);       \
       else if (mode == 2) k_direct<2, u64, KK, 4><<<g, kThreads, 0, st>>>(jd, s0, nslices);     \
+      else if (mode == 3) k_direct<3, u64, KK, 4><<<g, kThreads, 0, st>>>(jd, s0, nslices);     \
       else k_direct<1, float, KK, 4><<<g, kThreads, 0, st>>>(jd, s0, nslices);                  \
     } else {                                                                                     \
       if (mode == 0) k_direct<0, double, KK, 1><<<g, kThreads, 0, st>>>(jd, s0, nslices);       \
       else if (mode == 2) k_direct<2, u64, KK, 1><<<g, kThreads, 0, st>>>(jd, s0, nslices);     \
+      else if (mode == 3) k_direct<3, u64, KK, 1><<<g, kThreads, 0, st>>>(jd, s0, nslices);     \
       else k_direct<1, float, KK, 1><<<g, kThreads, 0, st>>>(jd, s0, nslices);                  \
     }
     switch (jd.kb) {
@@ -1872,12 +1929,14 @@ cudaError_t launch_once_list(int mode, const OnceList& ol, cudaStream_t st) {
   int per_sm = 0;
   cudaError_t e = mode == 0   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<0, double>, kThreads, 0)
                   : mode == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<2, u64>, kThreads, 0)
+                  : mode == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<3, u64>, kThreads, 0)
                               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_once_list<1, float>, kThreads, 0);
   if (e != cudaSuccess || per_sm < 1) per_sm = 1;
   const int64_t wave = (int64_t)sms * per_sm;
   const int grid = (int)(ol.total_tiles < wave ? ol.total_tiles : wave);
   if (mode == 0) k_once_list<0, double><<<grid, kThreads, 0, st>>>(ol);
   else if (mode == 2) k_once_list<2, u64><<<grid, kThreads, 0, st>>>(ol);
+  else if (mode == 3) k_once_list<3, u64><<<grid, kThreads, 0, st>>>(ol);
   else k_once_list<1, float><<<grid, kThreads, 0, st>>>(ol);
   return cudaGetLastError();
 }
@@ -1891,12 +1950,14 @@ cudaError_t launch_root(int mode, const RootDesc& rd, const int64_t* s0, int nsl
   if (E <= 1024) {  // few root entries: a CTA per entry, slices across its threads
     if (mode == 0) k_root_tree<0, double><<<(unsigned)E, kThreads, 0, st>>>(rd, s0, nslices);
     else if (mode == 2) k_root_tree<2, u64><<<(unsigned)E, kThreads, 0, st>>>(rd, s0, nslices);
+    else if (mode == 3) k_root_tree<3, u64><<<(unsigned)E, kThreads, 0, st>>>(rd, s0, nslices);
     else k_root_tree<1, float><<<(unsigned)E, kThreads, 0, st>>>(rd, s0, nslices);
     return cudaGetLastError();
   }
   const int g = grid_for(E);
   if (mode == 0) k_root<0, double><<<g, kThreads, 0, st>>>(rd, s0, nslices);
   else if (mode == 2) k_root<2, u64><<<g, kThreads, 0, st>>>(rd, s0, nslices);
+  else if (mode == 3) k_root<3, u64><<<g, kThreads, 0, st>>>(rd, s0, nslices);
   else k_root<1, float><<<g, kThreads, 0, st>>>(rd, s0, nslices);
   return cudaGetLastError();
 }
@@ -1916,6 +1977,13 @@ cudaError_t launch_set_s0(int64_t* d_s0, int64_t value, cudaStream_t st) {
 cudaError_t launch_leaf_int(const double* v64, void* out, int64_t n, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   k_leaf_int<<<grid_for(n), kThreads, 0, st>>>(v64, (u64*)out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_leaf_mod(const double* v64, void* out, int64_t n, uint64_t p, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  if (p < 2 || p >= (1ull << 28)) return cudaErrorInvalidValue;
+  k_leaf_mod<<<grid_for(n), kThreads, 0, st>>>(v64, (u64*)out, n, (long long)p);
   return cudaGetLastError();
 }
 

@@ -63,7 +63,7 @@ struct Node {
   std::vector<int> m_lsb, n_lsb, k_lsb;     // GEMM bit order, least significant first
   int64_t off = -1;              // arena offset (elements), joins only
   int kernel = togb::K_DIRECT;
-  int kernel_set[3] = {-1, -1, -1}; // per-form kernel chosen by the caller (togb_program_set_kernel), -1 = default
+  int kernel_set[4] = {-1, -1, -1, -1}; // per-form kernel chosen by the caller (togb_program_set_kernel), -1 = default
   bool dep = true;               // depends on the slice (reads a sliced leaf, directly or below)
   int slot = -1;                 // joins: index among the joins of its phase (metadata row)
 };
@@ -159,6 +159,11 @@ struct togb_program {
   // by the first int-form run after the leaves were created or replaced.
   void* d_leaf_int = nullptr;
   bool leaf_int_current = false;
+  // Residue form: the same integers modulo `modulus` (togb_program_set_modulus),
+  // converted for the modulus in `leaf_mod_p` (0 = not converted).
+  void* d_leaf_mod = nullptr;
+  uint64_t leaf_mod_p = 0;
+  uint64_t modulus = 0;
   // planning
   int64_t arena = 0;       // per-slice elements (slice-dependent joins)
   int64_t arena_once = 0;  // elements of the slice-invariant joins, shared by all slices
@@ -167,7 +172,9 @@ struct togb_program {
   int max_rank = 0;
   // device state
   double* d_acc = nullptr;  // [2 * 2^root_rank]: sum then compensation (int form: wrapping words, then zeros)
-  int acc_kind = 0;         // what the accumulator holds since the last reset: 0 nothing, 1 FP64 sums, 2 int words
+  int acc_kind = 0;         // what the accumulator holds since the last reset: 0 nothing, 1 FP64 sums,
+                            // 2 int words, 3 residues modulo acc_modulus
+  uint64_t acc_modulus = 0;
   int64_t* d_s0 = nullptr;
   int32_t* d_err = nullptr; // set by a kernel whose bounded wait expired
   int64_t wait_cycles = togb::kDefaultWaitCycles;  // limit of every device-side pipeline wait
@@ -216,7 +223,9 @@ namespace {
 
 size_t elem_size(int mode) { return mode == TOGB_MODE_SPLIT ? 4 : 8; }
 
-bool known_mode(int mode) { return mode == TOGB_MODE_F64 || mode == TOGB_MODE_SPLIT || mode == TOGB_MODE_INT64; }
+bool known_mode(int mode) {
+  return mode == TOGB_MODE_F64 || mode == TOGB_MODE_SPLIT || mode == TOGB_MODE_INT64 || mode == TOGB_MODE_MOD;
+}
 
 int64_t round256(int64_t x) { return (x + 255) / 256 * 256; }
 
@@ -463,6 +472,7 @@ void fill_operand(const togb_program* p, const Node& X, const std::vector<int>& 
   if (X.leaf >= 0) {
     const char* base = mode == TOGB_MODE_F64     ? (const char*)p->d_leaf64
                        : mode == TOGB_MODE_INT64 ? (const char*)p->d_leaf_int
+                       : mode == TOGB_MODE_MOD   ? (const char*)p->d_leaf_mod
                                                  : (const char*)p->d_leaf32;
     od.ptr = base + p->leaf_off[X.leaf] * es;
     od.batch_stride = 0;
@@ -706,6 +716,10 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
     jd.c_natural = is_natural(jd);
     jd.err = p->d_err;
     jd.wait_cycles = p->wait_cycles;
+    if (mode == TOGB_MODE_MOD && p->modulus >= 2) {  // runs require a modulus; describe may lack one
+      jd.mod_p = p->modulus;
+      jd.mod_m = ~0ull / p->modulus;
+    }
     if (mode == TOGB_MODE_SPLIT) {
       jd.c_exp = J.dep ? w.per_exp + (int64_t)J.slot * B : w.once_exp + J.slot;
       jd.c_max = J.dep ? w.per_max + (int64_t)J.slot * B : w.once_max + J.slot;
@@ -727,6 +741,10 @@ void build_descs(togb_program* p, int mode, void* ws_v, int B) {
   fill_operand(p, Rn, ref_lsb, {}, mode, ws, B, p->rd.r);
   p->rd.acc_sum = p->d_acc;
   p->rd.acc_comp = p->d_acc + pow2(Rn.rank);
+  if (mode == TOGB_MODE_MOD && p->modulus >= 2) {
+    p->rd.mod_p = p->modulus;
+    p->rd.mod_m = ~0ull / p->modulus;
+  }
   fuse_root(p, mode);
   if (mode == TOGB_MODE_SPLIT) {
     const WsLayout w = ws_layout(p, mode, ws, B);
@@ -856,6 +874,8 @@ togb_status prepare_once_fused(togb_program* p, int mode) {
       o.b_k = jd.b.r_k;
       o.inv_m = jd.r_inv_m;
       o.inv_n = jd.r_inv_n;
+      o.mod_p = jd.mod_p;
+      o.mod_m = jd.mod_m;
       const int64_t outs = pow2(jd.mb + jd.nb);
       const int64_t tiles = (outs + togb::kOnceTile - 1) / togb::kOnceTile;
       if ((int64_t)tf[i] + tiles > INT32_MAX / 2) return fail(TOGB_ERR_UNSUPPORTED, "slice-invariant phase too large to fuse");
@@ -1346,7 +1366,8 @@ togb_status togb_program_set_leaves(togb_program* p, const togb_leaf_spec* specs
         togb::launch_build_leaves(p->d_items, (int)p->h_items.size(), p->d_leaf64, p->d_leaf32, p->d_leaf32lo, st);
     if (e != cudaSuccess) return cuda_fail(e, "leaf build");
   }
-  p->leaf_int_current = false;  // the int form converts the new values at its next run
+  p->leaf_int_current = false;  // the int forms convert the new values at their next run
+  p->leaf_mod_p = 0;
   if (shift != p->leaf_shift) {  // the normalisers are part of the descriptors: rebuild them
     p->leaf_shift = shift;
     clear_graphs(p);
@@ -1421,7 +1442,7 @@ togb_status togb_program_info_get(const togb_program* p, togb_program_info* info
   info->num_launches = (int32_t)p->per.size() + 1;
   info->flops_per_slice = p->flops;
   info->bytes_per_slice_f64 = p->bytes64;
-  for (int m = 0; m < 3; ++m) {
+  for (int m = 0; m < 4; ++m) {
     info->workspace_per_slice[m] = ws_per_slice(p, m);
     info->workspace_fixed[m] = ws_fixed(p, m);
   }
@@ -1530,26 +1551,39 @@ togb_status togb_program_run(togb_program* p, int mode, int64_t begin, int64_t e
   if (p->host_only) return fail(TOGB_ERR_UNSUPPORTED, "host-only program: create it with togb_program_create to run it");
   if (!known_mode(mode)) return fail(TOGB_ERR_INVALID, "unknown mode");
   if (begin < 0 || end > p->num_slices || begin > end) return fail(TOGB_ERR_INVALID, "slice range out of bounds");
-  const int kind = mode == TOGB_MODE_INT64 ? 2 : 1;
-  if (p->acc_kind != 0 && p->acc_kind != kind)
-    return fail(TOGB_ERR_INVALID, kind == 2 ? "the accumulator holds FP64 sums: reset it before an int-form run"
-                                            : "the accumulator holds int-form words: reset it before an FP64 or split run");
+  const int kind = mode == TOGB_MODE_INT64 ? 2 : mode == TOGB_MODE_MOD ? 3 : 1;
+  if (kind == 3 && p->modulus < 2) return fail(TOGB_ERR_INVALID, "set a modulus (togb_program_set_modulus) first");
+  if (p->acc_kind != 0 && (p->acc_kind != kind || (kind == 3 && p->acc_modulus != p->modulus))) {
+    const std::string holds = p->acc_kind == 1   ? "FP64 sums"
+                              : p->acc_kind == 2 ? "int-form words"
+                                                 : "residues modulo " + std::to_string(p->acc_modulus);
+    return fail(TOGB_ERR_INVALID, "the accumulator holds " + holds + ": reset it first");
+  }
   if (begin == end) return TOGB_OK;
   cudaStream_t st = (cudaStream_t)stream_v;
   TOGB_CUDA(cudaSetDevice(p->device));
-  if (mode == TOGB_MODE_INT64 && !p->leaf_int_current) {
-    if (!p->d_leaf_int) {  // allocated once: descriptors keep its address
-      cudaError_t e = cudaMalloc(&p->d_leaf_int, std::max<int64_t>(p->num_leaf_values, 1) * 8);
-      if (e != cudaSuccess) {
-        p->d_leaf_int = nullptr;
-        return cuda_fail(e, "int-form leaf allocation");
+  if (kind >= 2) {
+    // The int forms' leaves, made from the FP64 values on this stream.  Each
+    // buffer is allocated once, so descriptors keep its address.
+    const bool mod = kind == 3;
+    void*& buf = mod ? p->d_leaf_mod : p->d_leaf_int;
+    if (mod ? p->leaf_mod_p != p->modulus : !p->leaf_int_current) {
+      if (!buf) {
+        cudaError_t e = cudaMalloc(&buf, std::max<int64_t>(p->num_leaf_values, 1) * 8);
+        if (e != cudaSuccess) {
+          buf = nullptr;
+          return cuda_fail(e, "int-form leaf allocation");
+        }
       }
+      cudaError_t e = mod ? togb::launch_leaf_mod(p->d_leaf64, buf, p->num_leaf_values, p->modulus, st)
+                          : togb::launch_leaf_int(p->d_leaf64, buf, p->num_leaf_values, st);
+      if (e != cudaSuccess) return cuda_fail(e, "int-form leaf conversion");
+      if (mod) p->leaf_mod_p = p->modulus;
+      else p->leaf_int_current = true;
     }
-    cudaError_t e = togb::launch_leaf_int(p->d_leaf64, p->d_leaf_int, p->num_leaf_values, st);
-    if (e != cudaSuccess) return cuda_fail(e, "int-form leaf conversion");
-    p->leaf_int_current = true;
   }
   p->acc_kind = kind;
+  p->acc_modulus = kind == 3 ? p->modulus : 0;
   const int64_t per = ws_per_slice(p, mode);
   const int64_t fixed = ws_fixed(p, mode);
   const int64_t want = end - begin;
@@ -1607,8 +1641,8 @@ togb_status result_ready(togb_program* p, void* stream, const void* out, int64_t
   if (p->host_only) return fail(TOGB_ERR_UNSUPPORTED, "host-only program has no result");
   const int64_t E = pow2(p->nodes[p->root].rank);
   if (n != E) return fail(TOGB_ERR_INVALID, "result size does not match the root tensor");
-  if (p->acc_kind != 0 && p->acc_kind != kind)
-    return fail(TOGB_ERR_INVALID, kind == 2 ? "the accumulator holds FP64 sums: read it with togb_program_result"
+  if (p->acc_kind != 0 && (p->acc_kind == 1) != (kind == 1))
+    return fail(TOGB_ERR_INVALID, kind != 1 ? "the accumulator holds FP64 sums: read it with togb_program_result"
                                             : "the accumulator holds int-form words: read it with togb_program_result_u64");
   TOGB_CUDA(cudaSetDevice(p->device));
   TOGB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
@@ -1624,6 +1658,19 @@ togb_status result_ready(togb_program* p, void* stream, const void* out, int64_t
 }
 
 }  // namespace
+
+togb_status togb_program_set_modulus(togb_program* p, uint64_t modulus) {
+  if (!p) return fail(TOGB_ERR_INVALID, "null program");
+  if (modulus < 2 || modulus >= (1ull << 28)) return fail(TOGB_ERR_INVALID, "the modulus must lie in [2, 2^28)");
+  if (modulus != p->modulus) {
+    p->modulus = modulus;
+    if (p->cur_mode == TOGB_MODE_MOD) {  // descriptors and graphs carry the modulus
+      clear_graphs(p);
+      p->cur_mode = -1;
+    }
+  }
+  return TOGB_OK;
+}
 
 togb_status togb_program_result_u64(togb_program* p, void* stream, uint64_t* out, int64_t n) {
   togb_status r = result_ready(p, stream, out, n, 2);
@@ -1657,6 +1704,7 @@ void togb_program_destroy(togb_program* p) {
   cudaFree(p->d_leaf32);
   cudaFree(p->d_leaf32lo);
   cudaFree(p->d_leaf_int);
+  cudaFree(p->d_leaf_mod);
   cudaFree(p->d_acc);
   cudaFree(p->d_s0);
   cudaFree(p->d_err);

@@ -17,6 +17,7 @@ from .program import Program
 MODE_F64 = 0
 MODE_SPLIT = 1
 MODE_INT64 = 2  # 64-bit integer words, sums and products modulo 2^64
+MODE_MOD = 3    # residues modulo the program's modulus (DeviceProgram.set_modulus)
 
 OK, ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_UNSUPPORTED, ERR_TIMEOUT = range(6)
 
@@ -47,8 +48,8 @@ class ProgramInfo(ctypes.Structure):
         ("num_launches", ctypes.c_int32),
         ("flops_per_slice", ctypes.c_double),
         ("bytes_per_slice_f64", ctypes.c_double),
-        ("workspace_per_slice", ctypes.c_int64 * 3),
-        ("workspace_fixed", ctypes.c_int64 * 3),
+        ("workspace_per_slice", ctypes.c_int64 * 4),
+        ("workspace_fixed", ctypes.c_int64 * 4),
         ("num_joins_once", ctypes.c_int32),
         ("pad_", ctypes.c_int32),
         ("flops_once", ctypes.c_double),
@@ -95,7 +96,7 @@ EXPORTS = [
     "togb_batch_create", "togb_batch_run", "togb_batch_results", "togb_batch_destroy",
     "togb_program_create_host", "togb_program_describe", "togb_program_create_compact",
     "togb_program_launch_count", "togb_program_set_wait_limit", "togb_program_set_leaves",
-    "togb_program_result_u64",
+    "togb_program_result_u64", "togb_program_set_modulus",
 ]
 
 KERNEL_NAMES = {0: "direct", 1: "tiled", 2: "reduce", 3: "tensor"}
@@ -125,6 +126,7 @@ def lib():
     L.togb_program_run.argtypes = [c_void, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, c_void, ctypes.c_size_t, c_void]
     L.togb_program_result.argtypes = [c_void, c_void, _f64p, _f64p, ctypes.c_int64]
     L.togb_program_result_u64.argtypes = [c_void, c_void, ctypes.POINTER(ctypes.c_uint64), ctypes.c_int64]
+    L.togb_program_set_modulus.argtypes = [c_void, ctypes.c_uint64]
     L.togb_program_set_timing.argtypes = [c_void, ctypes.c_int]
     L.togb_program_join_times.argtypes = [c_void, ctypes.POINTER(ctypes.c_float), ctypes.c_int32]
     L.togb_program_destroy.argtypes = [c_void]
@@ -359,9 +361,14 @@ class DeviceProgram:
         check(lib().togb_program_result(self._h, _stream_handle(stream), out.ctypes.data_as(_f64p), None, n))
         return out.reshape((2,) * int(self.info.root_rank))
 
+    def set_modulus(self, modulus):
+        """The residue form's modulus, in [2, 2^28)."""
+        check(lib().togb_program_set_modulus(self._h, int(modulus)))
+
     def result_words(self, stream=None, dtype=np.int64):
-        """The int form's accumulated root tensor: 64-bit words (the sums
-        modulo 2^64) read as ``dtype`` (``np.int64`` or ``np.uint64``)."""
+        """The int forms' accumulated root tensor: 64-bit words (the sums
+        modulo 2^64, or residues modulo the program's modulus) read as
+        ``dtype`` (``np.int64`` or ``np.uint64``)."""
         n = 1 << int(self.info.root_rank)
         out = np.zeros(n, dtype=np.uint64)
         check(lib().togb_program_result_u64(self._h, _stream_handle(stream),

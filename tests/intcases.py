@@ -17,12 +17,15 @@ MOD = 1 << 64
 
 def integer_weights(prog, w_neg=3, w_pos=5):
     """The same network with integer variable weights (stored as floats, as
-    the reference's weights are): counts far beyond 2^64, so every join and
-    the slice sum wrap."""
+    the reference's weights are) and dense leaves (partial contractions)
+    scaled by 8 and rounded up (zeros stay zeros): every leaf value an
+    integer, counts far beyond 2^64, so every join and the slice sum wrap."""
     out = copy.deepcopy(prog)
     for l in out.leaves:
         if l.kind == "var":
             l.w_neg, l.w_pos = float(w_neg), float(w_pos)
+        elif l.kind == "dense":
+            l.values = np.ceil(np.asarray(l.values, dtype=np.float64) * 8.0)
     return out
 
 

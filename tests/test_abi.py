@@ -32,6 +32,28 @@ def test_every_declared_symbol_is_exported(lib):
     assert set(syms) <= set(runtime.EXPORTS)
 
 
+def header_struct(name):
+    """(field, array length or 0) of a typedef struct in include/togb.h."""
+    with open(os.path.join(ROOT, "include", "togb.h")) as f:
+        text = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
+    body = re.search(r"typedef struct \{([^}]*)\}\s*" + name + r"\s*;", text).group(1)
+    out = []
+    for decl in body.split(";"):
+        for part in decl.strip().split(","):  # "double w_neg, w_pos" declares two fields
+            m = re.search(r"(\w+)\s*(?:\[(\d+)\])?\s*$", part.strip())
+            if m:
+                out.append((m.group(1), int(m.group(2) or 0)))
+    return out
+
+
+@pytest.mark.parametrize("mirror,name", [(runtime.ProgramInfo, "togb_program_info"),
+                                         (runtime.ProgramDesc, "togb_program_desc"),
+                                         (runtime.LeafSpec, "togb_leaf_spec")])
+def test_ctypes_mirrors_match_the_header(mirror, name):
+    fields = [(f, getattr(t, "_length_", 0)) for f, t in mirror._fields_]
+    assert fields == header_struct(name)
+
+
 def test_version(lib):
     assert lib.togb_version() == 1
 

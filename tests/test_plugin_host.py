@@ -29,8 +29,13 @@ def test_entry_types_and_sizes():
         q = api.GB300SplitAPI()
         q.add_argument("entry_type", name)
         assert q._mode == runtime.MODE_INT64 and q._word_type is word and q.get_entry_size() == 8
+    b = api.GB300SplitAPI()
+    b.add_argument("entry_type", "bigint")  # exact integers through the int forms
+    assert b._bigint and b.get_entry_size() == 8
+    b.add_argument("entry_type", "float32")
+    assert not b._bigint and b.get_entry_size() == 4
     with pytest.raises(ValueError):
-        p.add_argument("entry_type", "bigint")  # no device form, as in the reference's GPU backend
+        p.add_argument("entry_type", "complex128")
     with pytest.raises(ValueError):
         p.add_argument("tpu", "1.2.3.4")
     p.add_argument("thread_limit", 1)
