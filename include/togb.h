@@ -241,6 +241,12 @@ togb_status togb_tensordot_f64(const double* a, int32_t rank_a, const double* b,
                                int32_t n_axes, const int32_t* axes_a, const int32_t* axes_b,
                                double* out, void* stream);
 
+/* The same contraction of int64 tensors with sums and products modulo 2^64,
+ * as np.tensordot computes int64 (and, bit for bit, uint64) tensors. */
+togb_status togb_tensordot_i64(const int64_t* a, int32_t rank_a, const int64_t* b, int32_t rank_b,
+                               int32_t n_axes, const int32_t* axes_a, const int32_t* axes_b,
+                               int64_t* out, void* stream);
+
 /* Device throughput probe used for roofline denominators: runs `kind` on
  * every SM (0 = FP64 FMA chains, 1 = FP32 FMA chains, 2 = FP64 mma.sync
  * m8n8k4, 3 = tcgen05.mma kind::tf32 128x256x8) and returns the achieved

@@ -109,17 +109,30 @@ class GB300API:
         return np.full(shape, default_value, dtype=np.float64)
 
     def tensordot(self, a, b, axes):
-        """``np.tensordot`` on the device; numpy inputs are uploaded, the result
-        is a float64 CUDA tensor."""
+        """``np.tensordot`` on the device; numpy inputs are uploaded.  The
+        result is a float64 CUDA tensor, or for the ``int`` / ``uint`` entry
+        types an int64 one (64-bit words, sums and products modulo 2^64, as
+        numpy's int64 and uint64 tensordot gives them)."""
         import torch
 
         dev = torch.device("cuda", self._device)
+        words = self._mode == runtime.MODE_INT64 and not self._bigint
 
         def as_dev(x):
+            if words:
+                if isinstance(x, torch.Tensor):
+                    return x.to(device=dev, dtype=torch.int64)
+                v = np.asarray(x)
+                if v.dtype.kind == "f":
+                    v = v.astype(np.int64)  # toward zero, numpy's cast
+                return torch.as_tensor(np.ascontiguousarray(v.astype(np.uint64, copy=False).view(np.int64)),
+                                       device=dev)
             if isinstance(x, torch.Tensor):
                 return x.to(device=dev, dtype=torch.float64)
             return torch.as_tensor(np.asarray(x, dtype=np.float64), device=dev)
 
+        if words:
+            return runtime.tensordot_i64(as_dev(a), as_dev(b), axes)
         return runtime.tensordot_f64(as_dev(a), as_dev(b), axes)
 
     def warm(self):

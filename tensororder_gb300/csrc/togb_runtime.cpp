@@ -1868,8 +1868,12 @@ void togb_batch_destroy(togb_batch* b) {
 
 }  // extern "C"
 
-togb_status togb_tensordot_f64(const double* a, int32_t ra, const double* b, int32_t rb, int32_t n_axes,
-                               const int32_t* axes_a, const int32_t* axes_b, double* out, void* stream) {
+namespace {
+
+// One np.tensordot of binary-index tensors of 8-byte elements as a single
+// join in `mode` (TOGB_MODE_F64 or TOGB_MODE_INT64, which share the layout).
+togb_status tensordot_join(int mode, const void* a, int32_t ra, const void* b, int32_t rb, int32_t n_axes,
+                           const int32_t* axes_a, const int32_t* axes_b, void* out, void* stream) {
   if (!a || !b || !out) return fail(TOGB_ERR_INVALID, "null tensor");
   if (ra < 0 || rb < 0 || ra > 30 || rb > 30 || n_axes < 0 || n_axes > std::min(ra, rb))
     return fail(TOGB_ERR_INVALID, "bad ranks or axis count");
@@ -1930,9 +1934,21 @@ togb_status togb_tensordot_f64(const double* a, int32_t ra, const double* b, int
   jd.c_natural = is_natural(jd);
   jd.wait_cycles = togb::kDefaultWaitCycles;
   const int kernel = choose_kernel(jd.mb, jd.nb, jd.kb);
-  cudaError_t e = togb::launch_join(TOGB_MODE_F64, kernel, jd, nullptr, 1, (cudaStream_t)stream);
+  cudaError_t e = togb::launch_join(mode, kernel, jd, nullptr, 1, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "tensordot launch");
   return TOGB_OK;
+}
+
+}  // namespace
+
+togb_status togb_tensordot_f64(const double* a, int32_t ra, const double* b, int32_t rb, int32_t n_axes,
+                               const int32_t* axes_a, const int32_t* axes_b, double* out, void* stream) {
+  return tensordot_join(TOGB_MODE_F64, a, ra, b, rb, n_axes, axes_a, axes_b, out, stream);
+}
+
+togb_status togb_tensordot_i64(const int64_t* a, int32_t ra, const int64_t* b, int32_t rb, int32_t n_axes,
+                               const int32_t* axes_a, const int32_t* axes_b, int64_t* out, void* stream) {
+  return tensordot_join(TOGB_MODE_INT64, a, ra, b, rb, n_axes, axes_a, axes_b, out, stream);
 }
 
 togb_status togb_probe_peak(int kind, void* stream, double* flops) {

@@ -96,7 +96,7 @@ EXPORTS = [
     "togb_batch_create", "togb_batch_run", "togb_batch_results", "togb_batch_destroy",
     "togb_program_create_host", "togb_program_describe", "togb_program_create_compact",
     "togb_program_launch_count", "togb_program_set_wait_limit", "togb_program_set_leaves",
-    "togb_program_result_u64", "togb_program_set_modulus",
+    "togb_program_result_u64", "togb_program_set_modulus", "togb_tensordot_i64",
 ]
 
 KERNEL_NAMES = {0: "direct", 1: "tiled", 2: "reduce", 3: "tensor"}
@@ -133,6 +133,7 @@ def lib():
     L.togb_program_destroy.restype = None
     L.togb_tensordot_f64.argtypes = [c_void, ctypes.c_int32, c_void, ctypes.c_int32, ctypes.c_int32,
                                      _i32p, _i32p, c_void, c_void]
+    L.togb_tensordot_i64.argtypes = L.togb_tensordot_f64.argtypes
     L.togb_probe_peak.argtypes = [ctypes.c_int, c_void, ctypes.POINTER(ctypes.c_double)]
     L.togb_contract_static_f64.argtypes = [ctypes.POINTER(ProgramDesc), c_void, c_void, c_void]
     L.togb_program_joins.argtypes = [c_void, ctypes.c_int, _i32p, ctypes.c_int32]
@@ -448,12 +449,26 @@ def tensordot_f64(a, b, axes, out=None, stream=None):
     """``np.tensordot(a, b, axes)`` for binary-index FP64 CUDA tensors (torch)."""
     import torch
 
+    return _tensordot(a, b, axes, out, stream, torch.float64, lib().togb_tensordot_f64)
+
+
+def tensordot_i64(a, b, axes, out=None, stream=None):
+    """``np.tensordot(a, b, axes)`` for binary-index int64 CUDA tensors (torch),
+    sums and products modulo 2^64 as numpy computes int64 and uint64 tensors."""
+    import torch
+
+    return _tensordot(a, b, axes, out, stream, torch.int64, lib().togb_tensordot_i64)
+
+
+def _tensordot(a, b, axes, out, stream, dtype, entry):
+    import torch
+
     axes_a, axes_b = [list(x) for x in axes]
     if len(axes_a) != len(axes_b):
         raise ValueError("shape-mismatch for sum")
     for t in (a, b):
-        if t.dtype != torch.float64 or not t.is_cuda:
-            raise TypeError("tensordot_f64 takes float64 CUDA tensors")
+        if t.dtype != dtype or not t.is_cuda:
+            raise TypeError("tensordot takes %s CUDA tensors" % dtype)
         if any(d != 2 for d in t.shape):
             raise ValueError("only binary (dimension-2) indices are supported")
     ra, rb = a.dim(), b.dim()
@@ -463,12 +478,12 @@ def tensordot_f64(a, b, axes, out=None, stream=None):
     b = b.contiguous()
     rank = ra + rb - 2 * len(axes_a)
     if out is None:
-        out = torch.empty((2,) * rank, dtype=torch.float64, device=a.device)
+        out = torch.empty((2,) * rank, dtype=dtype, device=a.device)
     aa = np.array(axes_a or [0], dtype=np.int32)
     bb = np.array(axes_b or [0], dtype=np.int32)
-    check(lib().togb_tensordot_f64(ctypes.c_void_p(a.data_ptr()), ra, ctypes.c_void_p(b.data_ptr()), rb,
-                                   len(axes_a), aa.ctypes.data_as(_i32p), bb.ctypes.data_as(_i32p),
-                                   ctypes.c_void_p(out.data_ptr()), _stream_handle(stream)))
+    check(entry(ctypes.c_void_p(a.data_ptr()), ra, ctypes.c_void_p(b.data_ptr()), rb,
+                len(axes_a), aa.ctypes.data_as(_i32p), bb.ctypes.data_as(_i32p),
+                ctypes.c_void_p(out.data_ptr()), _stream_handle(stream)))
     return out
 
 

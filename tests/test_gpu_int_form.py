@@ -146,3 +146,47 @@ def test_one_kind_of_sum_between_resets(cuda):
     assert w == oracle_words(prog)
     assert int(twice) == (2 * int(w)) % MOD
     assert abs(f - float(oracle.contract_sliced(prog))) <= 1e-12 * abs(f)
+
+
+def _word_case(rng, ra, rb, k):
+    """Random int64 tensors spanning the whole range, so products and sums wrap."""
+    a = rng.integers(-(1 << 63), (1 << 63) - 1, size=(2,) * ra, dtype=np.int64, endpoint=True)
+    b = rng.integers(-(1 << 63), (1 << 63) - 1, size=(2,) * rb, dtype=np.int64, endpoint=True)
+    return a, b, (list(rng.permutation(ra)[:k]), list(rng.permutation(rb)[:k]))
+
+
+def _check_words(a, b, axes, cuda):
+    import torch
+
+    want = np.tensordot(a, b, axes)
+    got = runtime.tensordot_i64(torch.as_tensor(a, device=cuda), torch.as_tensor(b, device=cuda), axes)
+    got = got.cpu().numpy()
+    assert got.dtype == np.int64 and got.shape == want.shape
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_tensordot_i64_wraps_like_numpy(seed, cuda):
+    rng = np.random.default_rng(1000 + seed)
+    ra, rb = int(rng.integers(0, 10)), int(rng.integers(0, 10))
+    k = int(rng.integers(0, min(ra, rb) + 1))
+    _check_words(*_word_case(rng, ra, rb, k), cuda)
+
+
+@pytest.mark.parametrize("ra,rb,k", [(10, 10, 5), (16, 16, 8), (14, 12, 6), (20, 14, 10), (12, 20, 4),
+                                     (8, 8, 0), (12, 12, 12)])
+def test_tensordot_i64_shapes(ra, rb, k, cuda):
+    rng = np.random.default_rng(ra * 1000 + rb * 10 + k)
+    _check_words(*_word_case(rng, ra, rb, k), cuda)
+
+
+@pytest.mark.parametrize("entry,dtype", [("int", np.int64), ("uint", np.uint64)])
+def test_plugin_tensordot_follows_the_entry_type(entry, dtype, cuda):
+    rng = np.random.default_rng(5)
+    a = rng.integers(0, np.iinfo(dtype).max, size=(2,) * 7, dtype=dtype, endpoint=True)
+    b = rng.integers(0, np.iinfo(dtype).max, size=(2,) * 6, dtype=dtype, endpoint=True)
+    axes = ([1, 4, 6], [5, 0, 2])
+    backend = api.GB300API()
+    backend.add_argument("entry_type", entry)
+    got = backend.tensordot(a, b, axes).cpu().numpy().view(dtype)
+    assert np.array_equal(got, np.tensordot(a, b, axes))
