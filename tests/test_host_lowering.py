@@ -72,3 +72,46 @@ def test_gemm_classification(m, n, k, plain, split):
         hp.close()
     assert mnk == sorted((m, n))
     assert got == (plain, split)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_int_forms_lower_like_the_plain_form(name):
+    """The int form and the residue form share the plain form's 8-byte layout
+    and kernels (no tensor-core kernel); the residue form describes and
+    counts launches before any modulus is set (its Barrett constant is filled
+    only once a modulus exists), and both forms need as much workspace as
+    the plain form."""
+    prog = Program.from_dict(load_golden(name)["program"])
+    hp = runtime.HostProgram(prog)
+    try:
+        plain = hp.joins(runtime.MODE_F64)
+        for mode in (runtime.MODE_INT64, runtime.MODE_MOD):
+            assert (hp.joins(mode) == plain).all()
+            for j in range(len(plain)):
+                assert not hp.kernel_allowed(mode, j, 3)
+                assert hp.kernel_allowed(mode, j, 1)
+                assert "kernel %d" % plain[j][3] in hp.describe(mode, j)
+            assert hp.info.workspace_per_slice[mode] == hp.info.workspace_per_slice[runtime.MODE_F64]
+            assert hp.info.workspace_fixed[mode] == hp.info.workspace_fixed[runtime.MODE_F64]
+        assert launch_plan(prog, runtime.MODE_MOD) == launch_plan(prog, runtime.MODE_F64)
+        assert launch_plan(prog, runtime.MODE_INT64) == launch_plan(prog, runtime.MODE_F64)
+    finally:
+        hp.close()
+
+
+def test_unknown_modes_are_rejected():
+    hp = runtime.HostProgram(Program.from_dict(load_golden("vc60_s4")["program"]))
+    try:
+        for mode in (-1, 4, 99):
+            with pytest.raises(runtime.TogbError):
+                hp.joins(mode)
+            with pytest.raises(runtime.TogbError):
+                hp.describe(mode, 0)
+            with pytest.raises(runtime.TogbError):
+                hp.kernel_allowed(mode, 0, 0)
+        for bad in (0, 1, 1 << 28):
+            with pytest.raises(runtime.TogbError):
+                runtime.check(runtime.lib().togb_program_set_modulus(hp._h, bad))
+        runtime.check(runtime.lib().togb_program_set_modulus(hp._h, 268435399))
+    finally:
+        hp.close()
