@@ -11,6 +11,11 @@ combined once at the end.  The reference's analogue is the JAX backend's
 
 The combine is deterministic: partials are gathered in rank order and added
 with a two-sum on the host, so the result does not depend on arrival order.
+
+The int forms shard the same way.  A rank's partial is its words (the int
+form's sums modulo 2^64, or the residue form's residues modulo p).  The
+combine adds them modulo 2^64 or p, which is exact in any order
+(:func:`contract_sharded_words`).
 """
 from __future__ import annotations
 
@@ -80,6 +85,61 @@ def contract_sharded(num_slices: int, run_range: Callable[[int, int], Partial], 
     if world == 1:
         return combine([mine])
     return combine(gather_partials(mine, group))
+
+
+def combine_words(parts: Sequence[np.ndarray], modulus: int = 0) -> np.ndarray:
+    """Sum of per-rank words modulo 2^64 (``modulus`` 0, the int form) or
+    modulo ``modulus`` (the residue form), as uint64."""
+    if not parts:
+        raise ValueError("no partials")
+    shape = np.shape(parts[0])
+    m = int(modulus) if modulus else 1 << 64
+    total = [0] * (int(np.prod(shape)) if shape else 1)
+    for w in parts:
+        for e, x in enumerate(np.asarray(w).astype(np.uint64, copy=False).ravel()):
+            total[e] = (total[e] + int(x)) % m
+    return np.array(total, dtype=np.uint64).reshape(shape)
+
+
+def gather_words(words: np.ndarray, group=None) -> List[np.ndarray]:
+    """All-gather every rank's 64-bit words (as int64 through torch.distributed,
+    gloo or NCCL); returns them as uint64 in rank order."""
+    import torch
+    import torch.distributed as dist
+
+    w = np.ascontiguousarray(np.asarray(words).astype(np.uint64, copy=False).view(np.int64).ravel())
+    backend = dist.get_backend(group)
+    dev = torch.device("cuda", torch.cuda.current_device()) if backend == "nccl" else torch.device("cpu")
+    mine = torch.from_numpy(w).to(dev)
+    bufs = [torch.empty_like(mine) for _ in range(dist.get_world_size(group))]
+    dist.all_gather(bufs, mine, group=group)
+    shape = np.shape(words)
+    return [b.cpu().numpy().view(np.uint64).reshape(shape) for b in bufs]
+
+
+def contract_sharded_words(num_slices: int, run_range: Callable[[int, int], np.ndarray], rank: int, world: int,
+                           modulus: int = 0, group=None) -> np.ndarray:
+    """An int-form count sharded by slice range: ``run_range(begin, end)``
+    returns this rank's words; their sum modulo 2^64 (or ``modulus``) is
+    returned on every rank."""
+    begin, end = slice_range(num_slices, rank, world)
+    mine = run_range(begin, end)
+    if world == 1:
+        return combine_words([mine], modulus)
+    return combine_words(gather_words(mine, group), modulus)
+
+
+def device_words_runner(device_program, mode, workspace=None, stream=None):
+    """``run_range`` for :func:`contract_sharded_words` on this rank's GPU, in
+    the int form or the residue form (whose modulus the program holds)."""
+
+    def run(begin, end):
+        device_program.reset(stream)
+        if end > begin:
+            device_program.run(mode, begin, end, workspace=workspace, stream=stream)
+        return device_program.result_words(stream, np.uint64)
+
+    return run
 
 
 def device_range_runner(device_program, mode, workspace=None, stream=None):

@@ -29,11 +29,12 @@ def integer_weights(prog, w_neg=3, w_pos=5):
     return out
 
 
-def exact_count(prog):
-    """The count in Python integers (no wrap): leaves converted toward zero as
-    numpy's float-to-int64 cast does, then contracted as object arrays."""
+def exact_count(prog, begin=0, end=None):
+    """The count in Python integers (no wrap) over slices [begin, end): leaves
+    converted toward zero as numpy's float-to-int64 cast does, then contracted
+    as object arrays."""
     total = 0
-    for s in range(prog.num_slices):
+    for s in range(begin, prog.num_slices if end is None else end):
         fixed = oracle.slice_values(prog, s)
         stack = []
         for t in prog.postorder:

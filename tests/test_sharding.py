@@ -81,3 +81,55 @@ def test_sharded_count_over_gloo_ranks(name, world):
     want = load_golden(name)["reference"]["float64"]
     assert len(set(vals.values())) == 1
     assert abs(vals[0] - want) <= 1e-13 * abs(want)
+
+
+def test_combine_words_is_modular():
+    top = np.array([np.iinfo(np.uint64).max], dtype=np.uint64)
+    assert sharding.combine_words([top, np.array([2], dtype=np.uint64)])[0] == 1
+    p = 268435399
+    assert sharding.combine_words([np.array([p - 1], dtype=np.uint64), np.array([5], dtype=np.uint64)], p)[0] == 4
+
+
+def _words_worker(rank, world, port, name, modulus, q):
+    import torch.distributed as dist
+
+    from intcases import MOD, exact_count, integer_weights
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        prog = integer_weights(Program.from_dict(load_golden(name)["program"]))
+        m = modulus or MOD
+
+        def run_range(b, e):  # the oracle stands in for this rank's GPU
+            return np.array([exact_count(prog, b, e) % m], dtype=np.uint64)
+
+        got = sharding.contract_sharded_words(prog.num_slices, run_range, rank, world, modulus)
+        q.put((rank, int(got[0])))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("name,world,modulus", [("wvc30_s3", 2, 0), ("vc60_s4", 3, 0), ("vc60_s4", 3, 268435399)])
+def test_sharded_int_count_over_gloo_ranks(name, world, modulus):
+    """Int-form words (modulo 2^64) and residues (modulo a prime) shard
+    exactly: the ranks' combined words equal the whole count's."""
+    import multiprocessing as mp
+    import socket
+
+    from intcases import MOD, exact_count, integer_weights
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_words_worker, args=(r, world, port, name, modulus, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    vals = dict(q.get(timeout=10) for _ in range(world))
+    want = exact_count(integer_weights(Program.from_dict(load_golden(name)["program"]))) % (modulus or MOD)
+    assert set(vals.values()) == {want}
