@@ -18,7 +18,7 @@ pytestmark = pytest.mark.skipif(not refload.available(), reason="reference check
 
 @pytest.mark.parametrize("library,entry,mode", [("gb300", "float64", 0), ("gb300-split", "float64", 1),
                                                 ("gb300", "float32", 1), ("gb300", "int", 2),
-                                                ("gb300-split", "uint", 2)])
+                                                ("gb300-split", "uint", 2), ("gb300", "bigint", "exact")])
 def test_cli_selects_plugin(library, entry, mode, monkeypatch, capsys):
     refload.load()
     from oracle import contract
@@ -27,7 +27,9 @@ def test_cli_selects_plugin(library, entry, mode, monkeypatch, capsys):
     calls = []
 
     def stub(self, prog, limit):
-        calls.append((prog.num_joins, prog.num_slices, self._mode))
+        calls.append((prog.num_joins, prog.num_slices, "exact" if self._bigint else self._mode))
+        if self._bigint:
+            return np.asarray(int(contract.contract_sliced(prog, limit, dtype=np.int64)), dtype=object)
         dtype = self._word_type if self._mode == 2 else np.float64
         return np.asarray(contract.contract_sliced(prog, limit, dtype=dtype))
 
