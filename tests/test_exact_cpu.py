@@ -82,6 +82,7 @@ class ResidueProgram:
         self.modulus = None
         self.mode = None
         self.calls = []
+        self.ranges = []
         ResidueProgram.made.append(self)
 
     def set_leaves(self, program, stream=None):
@@ -99,6 +100,7 @@ class ResidueProgram:
     def run(self, mode, begin=0, end=None, workspace=None, stream=None):
         self.mode = mode
         self.calls.append((mode, self.modulus))
+        self.ranges.append((mode, begin, end))
 
     def set_modulus(self, p):
         self.modulus = p
@@ -128,10 +130,14 @@ def fake(monkeypatch):
     return ResidueProgram
 
 
-def small_network(w_neg=3.0, w_pos=5.0):
+def small_network(w_neg=3.0, w_pos=5.0, groups=0):
     leaves = [Leaf([0, 1], "or", positive=[True, False]), Leaf([0], "var", w_neg=w_neg, w_pos=w_pos),
               Leaf([1], "var", w_neg=2.0, w_pos=7.0)]
-    return Program(leaves, [0, 1, -1, 2, -1], []).validate()
+    tokens = [0, 1, -1, 2, -1]
+    for i in range(groups):  # independent variables, one slice group each
+        leaves.append(Leaf([2 + i], "var", w_neg=1.0, w_pos=1.0))
+        tokens += [3 + i, -1]
+    return Program(leaves, tokens, [[2 + i] for i in range(groups)]).validate()
 
 
 @pytest.mark.parametrize("x", [0, 12345, (1 << 64) + 17, 3 ** 200, 7 ** 350 + 1])
@@ -154,3 +160,21 @@ def test_plugin_non_integer_leaves_give_the_fp64_count(fake):
     got = backend.contract_program(small_network(w_neg=0.25))
     assert type(got) is float and got == 7.0
     assert [m for m, _ in fake.made[0].calls] == [runtime.MODE_F64]
+
+
+def test_every_pass_honours_the_slice_limit(fake):
+    """``num_slice_limit`` keeps a prefix of the slices (``base_api.py:23-24``):
+    the bound, the int form and every residue pass cover the same prefix."""
+    fake.X = 3 ** 100
+    prog = small_network(groups=3)  # 8 slices
+    backend = api.GB300API()
+    backend.add_argument("entry_type", "bigint")
+    backend.slices_per_call = 2
+    backend.contract_program(prog, num_slice_limit=5)
+    ranges = fake.made[0].ranges
+    modes = sorted(set(m for m, _, _ in ranges))
+    assert runtime.MODE_SPLIT in modes and runtime.MODE_INT64 in modes and runtime.MODE_MOD in modes
+    for mode in (runtime.MODE_SPLIT, runtime.MODE_INT64):
+        mine = [(b, e) for m, b, e in ranges if m == mode]
+        assert mine[0][0] == 0 and mine[-1][1] == 5
+        assert all(e1 == b2 for (_, e1), (b2, _) in zip(mine, mine[1:]))
