@@ -228,6 +228,57 @@ def batch_line(args, dev):
             "steps": args.batch_steps, "form": "split", "graph": "one CUDA graph per step, 16 internal streams"}
 
 
+def int_forms_line(prog, dev, steps=3):
+    """The unweighted count of the same plan (every variable weight 1) in the
+    int forms: the int form (the count modulo 2^64) and the residue form (one
+    prime) per count with the plan resident, and the exact ``bigint`` count
+    through the plugin (split-form bound, int form, the primes the bound
+    needs, Chinese remainder theorem).  Host wall clock after one warm-up
+    count; not part of the headline metric."""
+    import copy
+
+    import torch
+
+    from tensororder_gb300 import api, exact, runtime
+
+    unweighted = copy.deepcopy(prog)
+    for leaf in unweighted.leaves:
+        if leaf.kind == "var":
+            leaf.w_neg, leaf.w_pos = 1.0, 1.0
+    out = {"workload": "the headline plan with every variable weight 1 (its unweighted count)"}
+    dp = runtime.DeviceProgram(unweighted, dev.index or 0)
+    try:
+        dp.set_modulus(exact.MODULI[0])
+        words = {}
+        for name, mode in (("int64", runtime.MODE_INT64), ("residue", runtime.MODE_MOD)):
+            ws = dp.allocate_workspace(mode, unweighted.num_slices, max_fraction=0.3)
+            ms = []
+            for i in range(1 + steps):
+                torch.cuda.synchronize(dev)
+                t0 = time.perf_counter()
+                dp.reset()
+                dp.run(mode, workspace=ws)
+                words[name] = int(dp.result_words(dtype=np.uint64).reshape(-1)[0])
+                if i:
+                    ms.append((time.perf_counter() - t0) * 1e3)
+            out[name + "_ms_per_count"] = float(np.mean(ms))
+            del ws
+    finally:
+        dp.close()
+    backend = api.GB300API(device=dev.index or 0)
+    backend.add_argument("entry_type", "bigint")
+    x = backend.contract_program(unweighted)  # warm-up: lowering, workspaces
+    ms = []
+    for _ in range(max(1, steps - 1)):
+        t0 = time.perf_counter()
+        x = backend.contract_program(unweighted)
+        ms.append((time.perf_counter() - t0) * 1e3)
+    out.update({"bigint_ms_per_count": float(np.mean(ms)), "bigint_bits": int(x).bit_length(),
+                "bigint_low_word_equals_int64": int(x) % (1 << 64) == words["int64"],
+                "bigint_residue_equals_residue_form": int(x) % exact.MODULI[0] == words["residue"]})
+    return out
+
+
 def run_reference(args, rank, world):
     doc, prog = load_workload()
     if rank != 0:
@@ -277,6 +328,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--no-int-forms", action="store_true")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -501,6 +553,11 @@ def main():
     }
     if not args.no_batch and world == 1:
         line["batch512"] = batch_line(args, dev)
+    if not args.no_int_forms and world == 1:
+        try:
+            line["int_forms"] = int_forms_line(prog, dev)
+        except Exception as exc:  # a side figure: it never costs the bench line
+            line["int_forms"] = {"error": "%s: %s" % (type(exc).__name__, exc)}
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if world > 1:
